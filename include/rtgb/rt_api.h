@@ -1,0 +1,169 @@
+/*
+ * rt_api.h — the C ABI of the GB300 ray-trace hot path.
+ *
+ * In the reference, the path is a Vulkan compute "material": a pipeline plus
+ * a descriptor set whose bindings are filled in add-order (UBO, target image,
+ * accumulation image, triangles, materials, BVH nodes, lights, spheres;
+ * src/main.cpp:144-153), dispatched once per frame
+ * (src/scene/ComputeModel.cpp:21-25, src/main.cpp:228) with a UBO update per
+ * frame (src/main.cpp:166-183). Errors are C++ exceptions
+ * (src/scene/ComputeMaterial.cpp:37,57; caught in src/main.cpp:449-457).
+ *
+ * Here the same path is a context (device + stream + scene registry), scenes
+ * uploaded once and kept resident in HBM, and stream-ordered render / trace
+ * calls. Every function returns an rt_status; no C++ exception crosses the
+ * ABI. Device pointers are plain CUDA device pointers; `stream` is a
+ * cudaStream_t passed as void* (NULL = the context's own stream).
+ *
+ * Threading: one context may be used from several host threads; the scene
+ * registry is locked internally. Calls on one stream execute in order.
+ */
+#ifndef RTGB_RT_API_H
+#define RTGB_RT_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "rt_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rt_status {
+  RT_SUCCESS = 0,
+  RT_ERR_INVALID_ARGUMENT = 1,
+  RT_ERR_OUT_OF_MEMORY = 2,
+  RT_ERR_CUDA = 3,
+  RT_ERR_NOT_FOUND = 4,
+  RT_ERR_INVALID_SCENE = 5,
+  RT_ERR_STACK_OVERFLOW = 6,
+  RT_ERR_TIMEOUT = 7,
+  RT_ERR_BUDGET = 8,
+  RT_ERR_BUSY = 9,
+  RT_ERR_INTERNAL = 10
+} rt_status;
+
+typedef struct rt_ctx rt_ctx;
+typedef uint32_t rt_scene_id;
+
+typedef struct rt_ctx_desc {
+  int device;                /* CUDA device ordinal */
+  uint64_t hbm_budget_bytes; /* resident-scene budget; 0 = 80% of free HBM */
+  uint32_t flags;            /* reserved, 0 */
+  uint32_t _reserved;
+} rt_ctx_desc;
+
+typedef struct rt_scene_info {
+  uint32_t triangles, materials, lights, spheres, nodes;
+  uint32_t depth;           /* levels of the BVH (root = 1) */
+  uint64_t device_bytes;    /* HBM held by the scene */
+  float build_ms;           /* GPU BVH build time (0 when nodes were uploaded) */
+  float relayout_ms;        /* traversal-layout build time */
+} rt_scene_info;
+
+/* Replaces VulkanApplicationContext + ComputeMaterial::init
+ * (src/app-context/VulkanApplicationContext.cpp:7-181,
+ *  src/scene/ComputeMaterial.cpp:15-26): device, stream and pipeline state. */
+rt_status rtCreate(rt_ctx **ctx, const rt_ctx_desc *desc);
+rt_status rtDestroy(rt_ctx *ctx);
+
+/* Last error message of the context (thread-safe copy held by the context);
+ * replaces the std::runtime_error text of the reference. */
+const char *rtGetLastError(rt_ctx *ctx);
+const char *rtStatusString(rt_status s);
+
+/* Replaces GpuModel::Scene (src/ray-tracing/RtScene.h:44-101) plus the five
+ * storage-buffer bundles bound at bindings 3-7 (src/main.cpp:88-106,148-152).
+ * Host arrays in the reference's std430 layouts are validated (finite
+ * vertices, indices in range, material types 0-3), copied to HBM and owned
+ * by the context afterwards.
+ *   nodes == NULL : the BVH is built on the GPU, node-for-node identical to
+ *                   Bvh::createBvh (src/ray-tracing/Bvh.h:141-209) run in a
+ *                   fresh process whose rand() was seeded with `bvh_seed`
+ *                   (the reference never seeds: 1).
+ *   nodes != NULL : a node array in the Bvh.h layout is uploaded as is
+ *                   (it must be a full binary tree rooted at node 0).
+ *   lights == NULL: the light list is derived from LightSource materials as
+ *                   RtScene.h:87-96 does (area = |v0 x v1| / 2).
+ * The traversal layout (children-pair nodes and triangles in leaf order) is
+ * derived on the GPU. The call returns when the scene is resident. */
+rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *triangles, uint32_t n_triangles,
+                        const rt_material *materials, uint32_t n_materials, const rt_bvh_node *nodes,
+                        uint32_t n_nodes, const rt_light *lights, uint32_t n_lights, const rt_sphere *spheres,
+                        uint32_t n_spheres, uint32_t bvh_seed, rt_scene_id *out);
+rt_status rtReleaseScene(rt_ctx *ctx, rt_scene_id scene);
+rt_status rtGetSceneInfo(rt_ctx *ctx, rt_scene_id scene, rt_scene_info *out);
+
+/* Copies the scene's BVH back in the Bvh.h node layout (n = 2*triangles-1). */
+rt_status rtDownloadBvh(rt_ctx *ctx, rt_scene_id scene, rt_bvh_node *host_out, uint32_t n);
+/* Copies the scene's light list back (n = info.lights). */
+rt_status rtDownloadLights(rt_ctx *ctx, rt_scene_id scene, rt_light *host_out, uint32_t n);
+
+/* Light list of RtScene.h:87-96 computed on the host (no GPU). Returns the
+ * number of lights; `out` may be NULL to count. */
+uint32_t rtLightsFromMaterials(const rt_triangle *triangles, uint32_t n, const rt_material *materials,
+                               uint32_t n_materials, rt_light *out);
+
+/* The UBO camera (ubo.camPos, src/main.cpp:39-47,174) as the shader turns it
+ * into rays (ray-trace-compute.comp:357-372: vfov 30, looks down -z, zxy
+ * swizzle). */
+rt_status rtCameraFromReference(const float cam_pos[3], uint32_t width, uint32_t height, rt_camera *out);
+/* A general pinhole: eye, target, up, vertical field of view in degrees;
+ * image row 0 is the top row. */
+rt_status rtCameraLookAt(const float eye[3], const float target[3], const float up[3], float vfov_deg,
+                         uint32_t width, uint32_t height, rt_camera *out);
+/* Stores the camera used by rtRender for this scene (the per-frame UBO
+ * write of src/main.cpp:174-180). */
+rt_status rtSetCamera(rt_ctx *ctx, rt_scene_id scene, const rt_camera *camera);
+
+/* One progressive render call: replaces ComputeModel::computeCommand
+ * (src/scene/ComputeModel.cpp:21-25) and the target->accumulation image copy
+ * (src/main.cpp:253-261). Accumulates params->spp samples per pixel into
+ * the caller's RGBA32F device image (width*height*4 floats, row-major) as a
+ * running mean starting at sample params->sample_index (0 resets), tracing
+ * params->max_bounces bounces per path. Stream-ordered. */
+rt_status rtRender(rt_ctx *ctx, rt_scene_id scene, const rt_render_params *params, float *d_rgba32f,
+                   void *stream);
+
+/* Closest-hit casting for a device batch of rays (the hit_bvh loop of
+ * ray-trace-compute.comp:262-311 as a stand-alone query). Stream-ordered. */
+rt_status rtTraceClosest(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,
+                         void *stream);
+/* rtTraceClosest with compatibility flags: RT_COMPAT_STACK16 replays the
+ * shader's 16-entry stack (comp:262,280), including its silent truncation. */
+rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,
+                           uint32_t flags, void *stream);
+/* The same with host arrays: copies in, traces and copies out in pipelined
+ * chunks; returns when h_hits is filled. Pinned host memory gives
+ * asynchronous DMA. */
+rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_rays, uint32_t n, rt_hit *h_hits);
+
+/* Waits for the stream (NULL: the context stream) and reports any error a
+ * kernel recorded since the last call (e.g. RT_ERR_STACK_OVERFLOW). */
+rt_status rtSynchronize(rt_ctx *ctx, void *stream);
+
+/* Ray segments (camera rays plus every secondary ray) traced by render calls
+ * of this context since the last reset; waits for the device. Replaces the
+ * reference's ms/frame print (src/main.cpp:403-412) as the throughput
+ * counter. */
+rt_status rtReadSegmentCounter(rt_ctx *ctx, uint64_t *out, int reset);
+
+/* ------------------------------------------------------------------ batches
+ * Many renders of uneven size in one launch. */
+typedef struct rt_render_job {
+  rt_scene_id scene;
+  uint32_t _pad;
+  rt_camera camera;
+  rt_render_params params;
+  float *d_rgba32f;
+} rt_render_job;
+
+/* Renders every job with one persistent launch; per job the result equals
+ * rtRender of that job alone. */
+rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTGB_RT_API_H */

@@ -1,0 +1,168 @@
+"""Test infrastructure (oracle) — NOT part of the product.
+
+ctypes access to the CPU oracle (liboracle.so, built from rt_oracle.cpp) and,
+where it was built, to the reference's own BVH builder (_ref/libref_bvh.so,
+built from the reference's src/ray-tracing/Bvh.h). Only the tests,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg import this module,
+and only as the checker / the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref_bvh.so")
+
+
+def build() -> None:
+    """Builds liboracle.so (and _ref when the reference checkout exists)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = ctypes.CDLL(LIB_PATH)
+    P, U32, I32, D = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_double
+    sigs = {
+        "oracle_glibc_rand": (None, [U32, U32, P]),
+        "oracle_build_bvh": (I32, [P, U32, P, U32, ctypes.POINTER(I32)]),
+        "oracle_sort_with_depth": (None, [P, P, U32, I32]),
+        "oracle_lights_from_materials": (U32, [P, U32, P, U32, P]),
+        "oracle_camera_from_reference": (None, [P, U32, U32, P]),
+        "oracle_trace": (I32, [P, U32, P, U32, P, U32, I32, I32, D, P, P, I32]),
+        "oracle_trace_f64": (I32, [P, U32, P, U32, P, U32, P, P, I32]),
+        "oracle_render": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
+        "oracle_render_f64": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
+        "oracle_max_threads": (I32, []),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+LIB = _load()
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_PATH)
+
+
+def ref_lib():
+    lib = ctypes.CDLL(REF_PATH)
+    lib.ref_create_bvh.restype = ctypes.c_int
+    lib.ref_create_bvh.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32]
+    lib.ref_layout.restype = ctypes.c_int
+    lib.ref_layout.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.ref_rand_sequence.restype = None
+    lib.ref_rand_sequence.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
+    return lib
+
+
+def ref_build_bvh(tris: np.ndarray, seed: int = 1) -> np.ndarray:
+    """The reference's own Bvh::createBvh (needs the reference checkout)."""
+    tris = np.ascontiguousarray(tris, np.float32)
+    out = np.zeros((2 * len(tris) - 1, 12), np.float32)
+    rc = ref_lib().ref_create_bvh(_p(tris), len(tris), _p(out), seed)
+    if rc != 0:
+        raise RuntimeError(f"ref_create_bvh failed ({rc})")
+    return out
+
+
+def build_bvh(tris: np.ndarray, seed: int = 1):
+    """The oracle's restatement of Bvh::createBvh. Returns (nodes, depth)."""
+    tris = np.ascontiguousarray(tris, np.float32)
+    out = np.zeros((2 * len(tris) - 1, 12), np.float32)
+    depth = ctypes.c_int()
+    rc = LIB.oracle_build_bvh(_p(tris), len(tris), _p(out), seed, ctypes.byref(depth))
+    if rc != 0:
+        raise RuntimeError("oracle_build_bvh failed")
+    return out, depth.value
+
+
+def glibc_rand(seed: int, count: int) -> np.ndarray:
+    out = np.zeros(count, np.int32)
+    LIB.oracle_glibc_rand(seed, count, _p(out))
+    return out
+
+
+def sort_with_depth(keys: np.ndarray, depth: int):
+    keys = np.ascontiguousarray(keys, np.float32).copy()
+    idx = np.arange(len(keys), dtype=np.uint32)
+    LIB.oracle_sort_with_depth(_p(keys), _p(idx), len(keys), depth)
+    return keys, idx
+
+
+def lights_from_materials(tris, mats) -> np.ndarray:
+    n = LIB.oracle_lights_from_materials(_p(tris), len(tris), _p(mats), len(mats), None)
+    out = np.zeros((max(n, 1), 2), np.float32)
+    LIB.oracle_lights_from_materials(_p(tris), len(tris), _p(mats), len(mats), _p(out))
+    return out[:n]
+
+
+def camera_from_reference(cam_pos, W: int, H: int) -> np.ndarray:
+    p = np.asarray(cam_pos, np.float32)
+    out = np.zeros(12, np.float32)
+    LIB.oracle_camera_from_reference(_p(p), W, H, _p(out))
+    return out
+
+
+def trace(tris, nodes, rays, mode: int = 0, stack_size: int = 16, slack: float = 1e-5, stats: bool = False,
+          threads: int = 0):
+    """Closest hit per ray. Returns hits (n,4 float32; col 0 is int32 bits) and optionally stats (n,4 uint32)."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    hits = np.zeros((len(rays), 4), np.float32)
+    st = np.zeros((len(rays), 4), np.uint32) if stats else None
+    LIB.oracle_trace(_p(tris), len(tris), _p(nodes), len(nodes), _p(rays), len(rays), mode, stack_size, slack,
+                     _p(hits), _p(st), threads)
+    return (hits, st) if stats else hits
+
+
+def trace_f64(tris, nodes, rays, threads: int = 0):
+    rays = np.ascontiguousarray(rays, np.float32)
+    tri = np.zeros(len(rays), np.int32)
+    tuv = np.zeros((len(rays), 3), np.float64)
+    LIB.oracle_trace_f64(_p(tris), len(tris), _p(nodes), len(nodes), _p(rays), len(rays), _p(tri), _p(tuv), threads)
+    return tri, tuv
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32),
+                ("max_bounces", ctypes.c_uint32), ("sample_index", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("_reserved", ctypes.c_uint32 * 2)]
+
+
+def render(tris, mats, nodes, lights, spheres, camera: np.ndarray, width: int, height: int, spp: int = 1,
+           max_bounces: int = 8, sample_index: int = 0, flags: int = 0, accum=None, f64: bool = False,
+           threads: int = 0):
+    """Progressive render (in place on `accum`, W*H*4). Returns (accum, segments)."""
+    lights = np.zeros((0, 2), np.float32) if lights is None else np.ascontiguousarray(lights, np.float32)
+    spheres = np.zeros((0, 8), np.float32) if spheres is None else np.ascontiguousarray(spheres, np.float32)
+    cam = np.ascontiguousarray(camera, np.float32).reshape(12)
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float64 if f64 else np.float32)
+    p = _Params(width, height, spp, max_bounces, sample_index, flags)
+    seg = ctypes.c_uint64()
+    fn = LIB.oracle_render_f64 if f64 else LIB.oracle_render
+    fn(_p(tris), len(tris), _p(mats), len(mats), _p(nodes), len(nodes), _p(lights) if len(lights) else None,
+       len(lights), _p(spheres) if len(spheres) else None, len(spheres), _p(cam), ctypes.addressof(p), _p(accum),
+       ctypes.byref(seg), threads)
+    return accum, seg.value
+
+
+def max_threads() -> int:
+    return LIB.oracle_max_threads()

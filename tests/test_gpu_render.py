@@ -1,0 +1,124 @@
+"""GPU render (bounce loop) against the oracle: images within 1e-4 mean
+absolute error per channel, using the reference's per-pixel RNG stream."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4  # image MAE per channel
+
+
+def cornell(rt, ctx, n_soup=12000, n_spheres=4, seed=1):
+    t, m, s = rt.gen_cornell(seed, n_soup, n_spheres, 0.2, 1.0)
+    sc = ctx.upload_scene(t, m, spheres=s)
+    return t, m, s, sc
+
+
+def gpu_render(sc, cam, W, H, **kw):
+    import torch
+    accum = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    sc.set_camera(cam)
+    sc.render(accum, W, H, **kw)
+    sc.ctx.synchronize()
+    return accum.cpu().numpy()
+
+
+def mae(a, b):
+    return np.abs(a.astype(np.float64) - b.astype(np.float64)).reshape(-1, 4).mean(axis=0)
+
+
+def test_render_matches_golden_64(rt, ctx):
+    t, m, s, sc = cornell(rt, ctx)
+    try:
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 64, 64)
+        img = gpu_render(sc, cam, 64, 64, spp=1, max_bounces=8)
+        gold = np.load(os.path.join(GOLDEN, "render_cornell_64.npy"))
+        assert (mae(img, gold) <= TOL).all()
+        img = gpu_render(sc, cam, 64, 64, spp=4, max_bounces=8,
+                         flags=rt.COMPAT_STACK16 | rt.COMPAT_LEN1 | rt.COMPAT_UNORM8)
+        gold = np.load(os.path.join(GOLDEN, "render_cornell_64_compat.npy"))
+        assert (mae(img, gold) <= TOL).all()
+    finally:
+        sc.release()
+
+
+def test_render_config0_vs_oracle(rt, orc, ctx):
+    """Config 0: 256x256, 1 spp, 8 bounces, 12,012 triangles."""
+    t, m, s, sc = cornell(rt, ctx, n_spheres=0)
+    try:
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 256, 256)
+        img = gpu_render(sc, cam, 256, 256, spp=1, max_bounces=8)
+        want, seg = orc.render(t, m, sc.bvh(), sc.lights(), None, cam.as_array(), 256, 256, spp=1, max_bounces=8)
+        err = mae(img, want)
+        assert (err <= TOL).all(), err
+        assert img[..., 3].min() == 1.0
+        # Segment counter = the oracle's count of traced segments.
+        ctx.segments(reset=True)
+        gpu_render(sc, cam, 256, 256, spp=1, max_bounces=8)
+        assert abs(ctx.segments(reset=True) - seg) <= 0.001 * seg
+    finally:
+        sc.release()
+
+
+@pytest.mark.parametrize("flags", ["SPHERE_OVERRIDE", "NO_SPHERES", "LEN1", "SHADE_SIMPLE", "UNORM8", "STACK16"])
+def test_render_compat_modes(rt, orc, ctx, flags):
+    t, m, s, sc = cornell(rt, ctx, n_soup=3000, n_spheres=6, seed=2)
+    try:
+        f = getattr(rt, "COMPAT_" + flags, None) or getattr(rt, flags)
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 96, 80)
+        img = gpu_render(sc, cam, 96, 80, spp=2, max_bounces=6, flags=f)
+        want, _ = orc.render(t, m, sc.bvh(), sc.lights(), s, cam.as_array(), 96, 80, spp=2, max_bounces=6, flags=f)
+        assert (mae(img, want) <= TOL).all()
+    finally:
+        sc.release()
+
+
+def test_progressive_accumulation_across_calls(rt, orc, ctx):
+    """Two calls of 2 spp (sample_index 0 then 2) equal one 4-spp render."""
+    import torch
+    t, m, s, sc = cornell(rt, ctx, n_soup=2000, n_spheres=2, seed=3)
+    try:
+        W, H = 64, 48
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
+        sc.set_camera(cam)
+        accum = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        sc.render(accum, W, H, spp=2, max_bounces=8, sample_index=0)
+        sc.render(accum, W, H, spp=2, max_bounces=8, sample_index=2)
+        ctx.synchronize()
+        one = gpu_render(sc, cam, W, H, spp=4, max_bounces=8)
+        assert np.array_equal(accum.cpu().numpy(), one)
+        want, _ = orc.render(t, m, sc.bvh(), sc.lights(), s, cam.as_array(), W, H, spp=4, max_bounces=8)
+        assert (mae(one, want) <= TOL).all()
+    finally:
+        sc.release()
+
+
+def test_reference_camera_and_two_bounces(rt, orc, ctx):
+    """The reference's own frame setup: UBO camera (comp:357-372), 2 bounces,
+    hit_bvh-only path (no spheres), 16-entry stack, lengths of 1."""
+    t, m, s, sc = cornell(rt, ctx, n_soup=1410, n_spheres=1, seed=4)
+    try:
+        W, H = 200, 150
+        cam = rt.camera_from_reference([1.8, 8.6, 1.1], W, H)
+        f = rt.COMPAT_STACK16 | rt.COMPAT_LEN1 | rt.COMPAT_NO_SPHERES
+        img = gpu_render(sc, cam, W, H, spp=3, max_bounces=2, flags=f)
+        want, _ = orc.render(t, m, sc.bvh(), sc.lights(), s, cam.as_array(), W, H, spp=3, max_bounces=2, flags=f)
+        assert (mae(img, want) <= TOL).all()
+    finally:
+        sc.release()
+
+
+def test_render_without_camera_is_an_error(rt, ctx):
+    import torch
+    t, m, s = rt.gen_cornell(1, 10)
+    sc = ctx.upload_scene(t, m)
+    try:
+        accum = torch.zeros((8, 8, 4), device="cuda")
+        with pytest.raises(rt.RtError):
+            sc.render(accum, 8, 8)
+    finally:
+        sc.release()

@@ -1,0 +1,653 @@
+// Host runtime behind the C ABI (include/rtgb/rt_api.h).
+//
+// A context owns one device, one stream, a device error word, a ring of
+// per-launch work counters and the registry of resident scenes. A scene is
+// one device allocation holding the reference-layout arrays (triangles,
+// materials, lights, spheres, Bvh.h nodes) and the derived traversal layout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "rt_internal.h"
+
+using namespace rtgb;
+
+namespace {
+
+constexpr uint32_t kCounterRing = 1024;
+
+struct Scene {
+  DevScene dev{};
+  void *slab = nullptr;
+  uint64_t bytes = 0;
+  rt_camera camera{};
+  bool has_camera = false;
+  float build_ms = 0.0f, relayout_ms = 0.0f;
+  uint64_t last_use = 0;
+};
+
+}  // namespace
+
+struct rt_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  std::mutex mu;
+  std::unordered_map<uint32_t, Scene *> scenes;
+  uint32_t next_id = 1;
+  std::string last_error;
+  uint32_t *d_err = nullptr;       // [0] kernel error bits
+  uint32_t *d_counters = nullptr;  // kCounterRing launch-private work counters
+  unsigned long long *d_segments = nullptr;
+  std::atomic<uint32_t> counter_slot{0};
+  uint64_t budget = 0, used = 0, tick = 0;
+  // Device staging for rtTraceClosestHost (two chunk buffers per aux stream).
+  void *stage[2] = {nullptr, nullptr};
+  size_t stage_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string tl_error;
+
+rt_status fail(rt_ctx *ctx, rt_status s, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->last_error = buf;
+  }
+  return s;
+}
+
+rt_status cuda_fail(rt_ctx *ctx, cudaError_t e, const char *what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? RT_ERR_OUT_OF_MEMORY : RT_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+#define CK(call, what)                              \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+inline bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+cudaStream_t pick_stream(rt_ctx *ctx, void *s) { return s ? (cudaStream_t)s : ctx->stream; }
+
+uint32_t *next_counter(rt_ctx *ctx) {
+  uint32_t slot = ctx->counter_slot.fetch_add(1) % kCounterRing;
+  return ctx->d_counters + slot;
+}
+
+// Structural check of a Bvh.h node array: a full binary tree rooted at 0 in
+// which every node is reached once and leaves name valid triangles. Returns
+// the depth (levels) or 0 when the array is malformed.
+uint32_t check_tree(const rt_bvh_node *nodes, uint32_t nn, uint32_t ntris, std::string &why) {
+  std::vector<uint8_t> seen(nn, 0);
+  std::vector<std::pair<uint32_t, uint32_t>> stack{{0u, 1u}};
+  uint32_t depth = 0, visited = 0;
+  while (!stack.empty()) {
+    auto [i, d] = stack.back();
+    stack.pop_back();
+    if (i >= nn || seen[i]) {
+      why = "node array is not a tree";
+      return 0;
+    }
+    seen[i] = 1;
+    visited++;
+    depth = std::max(depth, d);
+    const rt_bvh_node &n = nodes[i];
+    if (n.left == -1 && n.right == -1) {
+      if (n.object < 0 || (uint32_t)n.object >= ntris) {
+        why = "leaf names a triangle out of range";
+        return 0;
+      }
+    } else {
+      if (n.left < 0 || n.right < 0 || n.object != -1) {
+        why = "inner node must have two children and object -1";
+        return 0;
+      }
+      stack.push_back({(uint32_t)n.left, d + 1});
+      stack.push_back({(uint32_t)n.right, d + 1});
+    }
+  }
+  if (visited != nn) {
+    why = "node array has unreachable nodes";
+    return 0;
+  }
+  return depth;
+}
+
+Scene *find_scene(rt_ctx *ctx, rt_scene_id id) {
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return nullptr;
+  it->second->last_use = ++ctx->tick;
+  return it->second;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rtStatusString(rt_status s) {
+  switch (s) {
+    case RT_SUCCESS: return "success";
+    case RT_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case RT_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case RT_ERR_CUDA: return "CUDA error";
+    case RT_ERR_NOT_FOUND: return "scene not found";
+    case RT_ERR_INVALID_SCENE: return "invalid scene data";
+    case RT_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+    case RT_ERR_TIMEOUT: return "timed out";
+    case RT_ERR_BUDGET: return "HBM budget exceeded";
+    case RT_ERR_BUSY: return "busy";
+    case RT_ERR_INTERNAL: return "internal error";
+  }
+  return "unknown status";
+}
+
+const char *rtGetLastError(rt_ctx *ctx) {
+  if (!ctx) return "null context";
+  std::lock_guard<std::mutex> g(ctx->mu);
+  tl_error = ctx->last_error;
+  return tl_error.c_str();
+}
+
+rt_status rtCreate(rt_ctx **out, const rt_ctx_desc *desc) {
+  if (!out) return RT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  rt_ctx *ctx = new rt_ctx();
+  ctx->device = desc ? desc->device : 0;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux[0], cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux[1], cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_err, 64);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 64);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, sizeof(uint32_t) * kCounterRing);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_segments, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_segments, 0, sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    tl_error = std::string("rtCreate: ") + cudaGetErrorString(e);
+    rtDestroy(ctx);
+    return e == cudaErrorMemoryAllocation ? RT_ERR_OUT_OF_MEMORY : RT_ERR_CUDA;
+  }
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  ctx->budget = (desc && desc->hbm_budget_bytes) ? desc->hbm_budget_bytes : (uint64_t)(0.8 * (double)free_b);
+  *out = ctx;
+  return RT_SUCCESS;
+}
+
+rt_status rtDestroy(rt_ctx *ctx) {
+  if (!ctx) return RT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->scenes) {
+    cudaFree(kv.second->slab);
+    delete kv.second;
+  }
+  for (int i = 0; i < 2; i++) {
+    if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+    if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
+  }
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->d_counters) cudaFree(ctx->d_counters);
+  if (ctx->d_segments) cudaFree(ctx->d_segments);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return RT_SUCCESS;
+}
+
+uint32_t rtLightsFromMaterials(const rt_triangle *tris, uint32_t n, const rt_material *mats, uint32_t nm,
+                               rt_light *out) {
+  uint32_t k = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    uint32_t m = tris[i].material_index;
+    if (m < nm && mats[m].type == RT_MATERIAL_LIGHT) {
+      // area = length(cross(v0, v1)) * 0.5 (RtScene.h:93); this file is
+      // built with -ffp-contract=off, so each operation rounds separately.
+      const float *a = tris[i].v0, *b = tris[i].v1;
+      float x = a[1] * b[2] - b[1] * a[2];
+      float y = a[2] * b[0] - b[2] * a[0];
+      float z = a[0] * b[1] - b[0] * a[1];
+      float len = std::sqrt(x * x + y * y + z * z);
+      if (out) out[k] = rt_light{i, len * 0.5f};
+      k++;
+    }
+  }
+  return k;
+}
+
+rt_status rtCameraFromReference(const float cam_pos[3], uint32_t W, uint32_t H, rt_camera *out) {
+  if (!cam_pos || !out || W == 0 || H == 0) return RT_ERR_INVALID_ARGUMENT;
+  // comp:358-369 in fp32: theta = vfov*pi/180, h = tan(theta/2), viewport
+  // 2h high and W/H * 2h wide, origin = camPos.zxy * (-1, 1, 1).
+  const float vfov = 30.0f, pi = 3.1415926535897932385f;
+  float theta = vfov * pi / 180.0f;
+  float h = std::tan(theta / 2.0f);
+  float vh = 2.0f * h;
+  float vw = (float)W / (float)H * vh;
+  float hor[3] = {vw, 0.0f, 0.0f}, ver[3] = {0.0f, -vh, 0.0f};
+  float org[3] = {-cam_pos[2], cam_pos[0], cam_pos[1]};
+  float foc[3] = {0.0f, 0.0f, 1.0f};
+  for (int a = 0; a < 3; a++) {
+    out->origin[a] = org[a];
+    out->horizontal[a] = hor[a];
+    out->vertical[a] = ver[a];
+    out->lower_left[a] = org[a] - hor[a] / 2.0f - ver[a] / 2.0f - foc[a];
+  }
+  return RT_SUCCESS;
+}
+
+rt_status rtCameraLookAt(const float eye[3], const float target[3], const float up[3], float vfov_deg, uint32_t W,
+                         uint32_t H, rt_camera *out) {
+  if (!eye || !target || !up || !out || W == 0 || H == 0 || !(vfov_deg > 0.0f && vfov_deg < 180.0f))
+    return RT_ERR_INVALID_ARGUMENT;
+  // Computed in double and rounded once: the camera is an input to both
+  // the kernels and any checker, so only its stored fp32 values matter.
+  double f[3], r[3], u[3];
+  for (int a = 0; a < 3; a++) f[a] = (double)target[a] - (double)eye[a];
+  double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+  if (!(fl > 0.0)) return RT_ERR_INVALID_ARGUMENT;
+  for (double &x : f) x /= fl;
+  r[0] = f[1] * up[2] - f[2] * up[1];
+  r[1] = f[2] * up[0] - f[0] * up[2];
+  r[2] = f[0] * up[1] - f[1] * up[0];
+  double rl = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  if (!(rl > 0.0)) return RT_ERR_INVALID_ARGUMENT;
+  for (double &x : r) x /= rl;
+  u[0] = r[1] * f[2] - r[2] * f[1];
+  u[1] = r[2] * f[0] - r[0] * f[2];
+  u[2] = r[0] * f[1] - r[1] * f[0];
+  const double kPi = 3.14159265358979323846;
+  double vh = 2.0 * std::tan((double)vfov_deg * kPi / 360.0);
+  double vw = vh * (double)W / (double)H;
+  for (int a = 0; a < 3; a++) {
+    double hor = vw * r[a], ver = -vh * u[a];
+    out->origin[a] = eye[a];
+    out->horizontal[a] = (float)hor;
+    out->vertical[a] = (float)ver;
+    out->lower_left[a] = (float)((double)eye[a] + f[a] - 0.5 * hor - 0.5 * ver);
+  }
+  return RT_SUCCESS;
+}
+
+rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const rt_material *mats, uint32_t nm,
+                        const rt_bvh_node *nodes, uint32_t nn, const rt_light *lights, uint32_t nl,
+                        const rt_sphere *spheres, uint32_t ns, uint32_t bvh_seed, rt_scene_id *out) {
+  if (!ctx || !out) return RT_ERR_INVALID_ARGUMENT;
+  *out = 0;
+  if (!tris || nt == 0) return fail(ctx, RT_ERR_INVALID_SCENE, "a scene needs at least one triangle");
+  if (nt > (1u << 30)) return fail(ctx, RT_ERR_INVALID_SCENE, "too many triangles (%u)", nt);
+  if (!mats || nm == 0) return fail(ctx, RT_ERR_INVALID_SCENE, "a scene needs at least one material");
+  if ((ns && !spheres) || (nl && !lights && lights != nullptr))
+    return fail(ctx, RT_ERR_INVALID_ARGUMENT, "null array with nonzero count");
+  for (uint32_t i = 0; i < nm; i++) {
+    if (mats[i].type > RT_MATERIAL_GLASS) return fail(ctx, RT_ERR_INVALID_SCENE, "material %u: type %u", i, mats[i].type);
+    if (!finite3(mats[i].albedo) || !std::isfinite(mats[i].fuzz) || !std::isfinite(mats[i].ior) ||
+        mats[i].fuzz < 0.0f || mats[i].ior < 0.0f)
+      return fail(ctx, RT_ERR_INVALID_SCENE, "material %u: non-finite or negative parameter", i);
+  }
+  for (uint32_t i = 0; i < nt; i++) {
+    if (!finite3(tris[i].v0) || !finite3(tris[i].v1) || !finite3(tris[i].v2))
+      return fail(ctx, RT_ERR_INVALID_SCENE, "triangle %u: non-finite vertex", i);
+    if (tris[i].material_index >= nm)
+      return fail(ctx, RT_ERR_INVALID_SCENE, "triangle %u: material %u out of range", i, tris[i].material_index);
+  }
+  for (uint32_t i = 0; i < ns; i++) {
+    if (!finite3(spheres[i].s) || !std::isfinite(spheres[i].s[3]) || spheres[i].material_index >= nm)
+      return fail(ctx, RT_ERR_INVALID_SCENE, "sphere %u: bad centre, radius or material", i);
+  }
+  std::vector<rt_light> derived;
+  if (!lights) {
+    derived.resize(rtLightsFromMaterials(tris, nt, mats, nm, nullptr));
+    rtLightsFromMaterials(tris, nt, mats, nm, derived.data());
+    lights = derived.data();
+    nl = (uint32_t)derived.size();
+  }
+  for (uint32_t i = 0; i < nl; i++)
+    if (lights[i].triangle_index >= nt) return fail(ctx, RT_ERR_INVALID_SCENE, "light %u: triangle out of range", i);
+  const uint32_t nnodes = 2 * nt - 1;
+  uint32_t depth = 0;
+  if (nodes) {
+    if (nn != nnodes) return fail(ctx, RT_ERR_INVALID_SCENE, "expected %u nodes, got %u", nnodes, nn);
+    std::string why;
+    depth = check_tree(nodes, nn, nt, why);
+    if (!depth) return fail(ctx, RT_ERR_INVALID_SCENE, "%s", why.c_str());
+    if (depth > 64) return fail(ctx, RT_ERR_INVALID_SCENE, "tree depth %u exceeds 64", depth);
+  }
+
+  // One slab per scene.
+  const uint32_t ninner = nt > 1 ? nt - 1 : 1;
+  size_t off_tris = 0;
+  size_t off_mats = off_tris + align256(sizeof(rt_triangle) * nt);
+  size_t off_lights = off_mats + align256(sizeof(rt_material) * nm);
+  size_t off_spheres = off_lights + align256(sizeof(rt_light) * std::max(nl, 1u));
+  size_t off_nodes = off_spheres + align256(sizeof(rt_sphere) * std::max(ns, 1u));
+  size_t off_bvh2 = off_nodes + align256(sizeof(rt_bvh_node) * nnodes);
+  size_t off_tpre = off_bvh2 + align256(64ull * ninner);
+  size_t off_leaf = off_tpre + align256(48ull * nt);
+  size_t total = off_leaf + align256(4ull * nt);
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (ctx->used + total > ctx->budget)
+      return RT_ERR_BUDGET;
+    ctx->used += total;
+  }
+  auto unreserve = [&]() {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->used -= total;
+  };
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  char *slab = nullptr;
+  cudaError_t e = cudaMalloc((void **)&slab, total);
+  if (e != cudaSuccess) {
+    unreserve();
+    return cuda_fail(ctx, e, "scene allocation");
+  }
+  Scene *sc = new Scene();
+  sc->slab = slab;
+  sc->bytes = total;
+  DevScene &d = sc->dev;
+  d.tris = (const rt_triangle *)(slab + off_tris);
+  d.mats = (const rt_material *)(slab + off_mats);
+  d.lights = (const rt_light *)(slab + off_lights);
+  d.spheres = (const rt_sphere *)(slab + off_spheres);
+  d.nodes = (const rt_bvh_node *)(slab + off_nodes);
+  d.bvh2 = (const float4 *)(slab + off_bvh2);
+  d.tpre = (const float4 *)(slab + off_tpre);
+  d.leaf_tri = (const int32_t *)(slab + off_leaf);
+  d.ntris = nt;
+  d.nmats = nm;
+  d.nlights = nl;
+  d.nspheres = ns;
+  d.nnodes = nnodes;
+  cudaStream_t st = ctx->stream;
+  auto abort_upload = [&](rt_status s) {
+    cudaStreamSynchronize(st);
+    cudaFree(slab);
+    delete sc;
+    unreserve();
+    return s;
+  };
+#define UCK(call, what)                                                   \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) return abort_upload(cuda_fail(ctx, e_, what)); \
+  } while (0)
+  UCK(cudaMemcpyAsync(slab + off_tris, tris, sizeof(rt_triangle) * nt, cudaMemcpyHostToDevice, st), "upload triangles");
+  UCK(cudaMemcpyAsync(slab + off_mats, mats, sizeof(rt_material) * nm, cudaMemcpyHostToDevice, st), "upload materials");
+  if (nl) UCK(cudaMemcpyAsync(slab + off_lights, lights, sizeof(rt_light) * nl, cudaMemcpyHostToDevice, st), "upload lights");
+  if (ns) UCK(cudaMemcpyAsync(slab + off_spheres, spheres, sizeof(rt_sphere) * ns, cudaMemcpyHostToDevice, st), "upload spheres");
+  rt_bvh_node *dnodes = (rt_bvh_node *)(slab + off_nodes);
+  if (nodes) {
+    UCK(cudaMemcpyAsync(dnodes, nodes, sizeof(rt_bvh_node) * nnodes, cudaMemcpyHostToDevice, st), "upload nodes");
+  } else {
+    std::vector<uint8_t> axes(nnodes);
+    glibc_rand_axes(bvh_seed, nnodes, axes.data());
+    char errbuf[256] = {0};
+    rt_status bs = gpu_build_bvh((const rt_triangle *)(slab + off_tris), nt, axes.data(), dnodes, st, &sc->build_ms,
+                                 &depth, errbuf, sizeof(errbuf));
+    if (bs != RT_SUCCESS) return abort_upload(fail(ctx, bs, "%s", errbuf));
+  }
+  d.depth = depth;
+  if (depth > 64) return abort_upload(fail(ctx, RT_ERR_INVALID_SCENE, "tree depth %u exceeds 64", depth));
+  // Traversal layout.
+  {
+    uint32_t *scratch = nullptr;
+    size_t words = 2ull * nnodes + nnodes / 1024 + 2;
+    UCK(cudaMallocAsync((void **)&scratch, 4 * words, st), "relayout scratch");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, st);
+    cudaError_t le = launch_relayout(dnodes, nnodes, d.tris, (float4 *)d.bvh2, (float4 *)d.tpre,
+                                     (int32_t *)d.leaf_tri, scratch, st);
+    cudaEventRecord(b, st);
+    cudaFreeAsync(scratch, st);
+    if (le != cudaSuccess) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return abort_upload(cuda_fail(ctx, le, "relayout"));
+    }
+    rt_bvh_node root;
+    UCK(cudaMemcpyAsync(&root, dnodes, sizeof(root), cudaMemcpyDeviceToHost, st), "read root");
+    UCK(cudaStreamSynchronize(st), "upload");
+    cudaEventElapsedTime(&sc->relayout_ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    for (int k = 0; k < 3; k++) {
+      d.root_lo[k] = root.min[k];
+      d.root_hi[k] = root.max[k];
+    }
+    d.root_ref = (root.left != -1) ? 0 : ~0;
+  }
+#undef UCK
+  std::lock_guard<std::mutex> g(ctx->mu);
+  uint32_t id = ctx->next_id++;
+  sc->last_use = ++ctx->tick;
+  ctx->scenes[id] = sc;
+  *out = id;
+  return RT_SUCCESS;
+}
+
+rt_status rtReleaseScene(rt_ctx *ctx, rt_scene_id id) {
+  if (!ctx) return RT_ERR_INVALID_ARGUMENT;
+  Scene *sc = nullptr;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return RT_ERR_NOT_FOUND;
+    sc = it->second;
+    ctx->scenes.erase(it);
+    ctx->used -= sc->bytes;
+  }
+  // Work already queued on any stream may still read the scene.
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  cudaFree(sc->slab);
+  delete sc;
+  return RT_SUCCESS;
+}
+
+rt_status rtGetSceneInfo(rt_ctx *ctx, rt_scene_id id, rt_scene_info *out) {
+  if (!ctx || !out) return RT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Scene *sc = find_scene(ctx, id);
+  if (!sc) return RT_ERR_NOT_FOUND;
+  out->triangles = sc->dev.ntris;
+  out->materials = sc->dev.nmats;
+  out->lights = sc->dev.nlights;
+  out->spheres = sc->dev.nspheres;
+  out->nodes = sc->dev.nnodes;
+  out->depth = sc->dev.depth;
+  out->device_bytes = sc->bytes;
+  out->build_ms = sc->build_ms;
+  out->relayout_ms = sc->relayout_ms;
+  return RT_SUCCESS;
+}
+
+rt_status rtDownloadBvh(rt_ctx *ctx, rt_scene_id id, rt_bvh_node *host_out, uint32_t n) {
+  if (!ctx || !host_out) return RT_ERR_INVALID_ARGUMENT;
+  DevScene d;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    Scene *sc = find_scene(ctx, id);
+    if (!sc) return RT_ERR_NOT_FOUND;
+    d = sc->dev;
+  }
+  if (n != d.nnodes) return fail(ctx, RT_ERR_INVALID_ARGUMENT, "expected %u nodes", d.nnodes);
+  CK(cudaMemcpyAsync(host_out, d.nodes, sizeof(rt_bvh_node) * n, cudaMemcpyDeviceToHost, ctx->stream), "download");
+  CK(cudaStreamSynchronize(ctx->stream), "download");
+  return RT_SUCCESS;
+}
+
+rt_status rtDownloadLights(rt_ctx *ctx, rt_scene_id id, rt_light *host_out, uint32_t n) {
+  if (!ctx || (!host_out && n)) return RT_ERR_INVALID_ARGUMENT;
+  DevScene d;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    Scene *sc = find_scene(ctx, id);
+    if (!sc) return RT_ERR_NOT_FOUND;
+    d = sc->dev;
+  }
+  if (n != d.nlights) return fail(ctx, RT_ERR_INVALID_ARGUMENT, "expected %u lights", d.nlights);
+  if (n == 0) return RT_SUCCESS;
+  CK(cudaMemcpyAsync(host_out, d.lights, sizeof(rt_light) * n, cudaMemcpyDeviceToHost, ctx->stream), "download");
+  CK(cudaStreamSynchronize(ctx->stream), "download");
+  return RT_SUCCESS;
+}
+
+rt_status rtSetCamera(rt_ctx *ctx, rt_scene_id id, const rt_camera *cam) {
+  if (!ctx || !cam) return RT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Scene *sc = find_scene(ctx, id);
+  if (!sc) return RT_ERR_NOT_FOUND;
+  sc->camera = *cam;
+  sc->has_camera = true;
+  return RT_SUCCESS;
+}
+
+rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t flags,
+                           void *stream);
+
+rt_status rtTraceClosest(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint32_t n, rt_hit *hits, void *stream) {
+  return rtTraceClosestEx(ctx, id, rays, n, hits, 0, stream);
+}
+
+rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t flags,
+                           void *stream) {
+  if (!ctx || (n && (!rays || !hits))) return RT_ERR_INVALID_ARGUMENT;
+  if ((uintptr_t)rays % 16 || (uintptr_t)hits % 16)
+    return fail(ctx, RT_ERR_INVALID_ARGUMENT, "ray and hit arrays must be 16-byte aligned");
+  if (flags & ~RT_COMPAT_STACK16) return fail(ctx, RT_ERR_INVALID_ARGUMENT, "unsupported trace flags");
+  DevScene d;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    Scene *sc = find_scene(ctx, id);
+    if (!sc) return RT_ERR_NOT_FOUND;
+    d = sc->dev;
+  }
+  if (n == 0) return RT_SUCCESS;
+  cudaStream_t st = pick_stream(ctx, stream);
+  cudaError_t e = (flags & RT_COMPAT_STACK16) ? launch_trace_literal16(d, rays, n, hits, st)
+                                               : launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
+  return RT_SUCCESS;
+}
+
+rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, uint32_t n, rt_hit *h_hits) {
+  if (!ctx || (n && (!h_rays || !h_hits))) return RT_ERR_INVALID_ARGUMENT;
+  DevScene d;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    Scene *sc = find_scene(ctx, id);
+    if (!sc) return RT_ERR_NOT_FOUND;
+    d = sc->dev;
+  }
+  if (n == 0) return RT_SUCCESS;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  // Chunks alternate between two streams so the copy of one chunk overlaps
+  // the traversal of the other.
+  const uint32_t chunk = 1u << 20;
+  const size_t need = (size_t)chunk * (sizeof(rt_ray) + sizeof(rt_hit));
+  if (ctx->stage_bytes < need) {
+    for (int i = 0; i < 2; i++) {
+      if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+      ctx->stage[i] = nullptr;
+      CK(cudaMalloc(&ctx->stage[i], need), "staging allocation");
+    }
+    ctx->stage_bytes = need;
+  }
+  for (uint32_t c = 0, k = 0; c < n; c += chunk, k++) {
+    uint32_t m = std::min(chunk, n - c);
+    int s = k & 1;
+    cudaStream_t st = ctx->aux[s];
+    rt_ray *dr = (rt_ray *)ctx->stage[s];
+    rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
+    CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
+    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, st), "trace launch");
+    CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
+  }
+  CK(cudaStreamSynchronize(ctx->aux[0]), "trace");
+  CK(cudaStreamSynchronize(ctx->aux[1]), "trace");
+  return rtSynchronize(ctx, nullptr);
+}
+
+rt_status rtRender(rt_ctx *ctx, rt_scene_id id, const rt_render_params *p, float *accum, void *stream) {
+  if (!ctx || !p || !accum) return RT_ERR_INVALID_ARGUMENT;
+  if ((uintptr_t)accum % 16) return fail(ctx, RT_ERR_INVALID_ARGUMENT, "image must be 16-byte aligned");
+  if (p->width == 0 || p->height == 0 || p->width > 65536 || p->height > 65536)
+    return fail(ctx, RT_ERR_INVALID_ARGUMENT, "bad image size %ux%u", p->width, p->height);
+  DevScene d;
+  rt_camera cam;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    Scene *sc = find_scene(ctx, id);
+    if (!sc) return RT_ERR_NOT_FOUND;
+    if (!sc->has_camera) {
+      ctx->last_error = "rtRender: no camera set for this scene (rtSetCamera)";
+      return RT_ERR_INVALID_ARGUMENT;
+    }
+    d = sc->dev;
+    cam = sc->camera;
+  }
+  cudaError_t e = launch_render(d, cam, *p, accum, ctx->d_segments, ctx->d_err, pick_stream(ctx, stream));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "render launch");
+  return RT_SUCCESS;
+}
+
+// Number of ray segments traced by render calls since the last reset
+// (waits for the context stream).
+rt_status rtReadSegmentCounter(rt_ctx *ctx, uint64_t *out, int reset) {
+  if (!ctx || !out) return RT_ERR_INVALID_ARGUMENT;
+  unsigned long long v = 0;
+  CK(cudaDeviceSynchronize(), "synchronize");
+  CK(cudaMemcpy(&v, ctx->d_segments, sizeof(v), cudaMemcpyDeviceToHost), "read counter");
+  if (reset) CK(cudaMemset(ctx->d_segments, 0, sizeof(v)), "reset counter");
+  *out = v;
+  return RT_SUCCESS;
+}
+
+rt_status rtSynchronize(rt_ctx *ctx, void *stream) {
+  if (!ctx) return RT_ERR_INVALID_ARGUMENT;
+  CK(cudaStreamSynchronize(pick_stream(ctx, stream)), "synchronize");
+  uint32_t bits = 0;
+  CK(cudaMemcpy(&bits, ctx->d_err, sizeof(bits), cudaMemcpyDeviceToHost), "read error word");
+  if (bits) {
+    CK(cudaMemset(ctx->d_err, 0, sizeof(bits)), "reset error word");
+    if (bits & KERR_STACK_OVERFLOW) return fail(ctx, RT_ERR_STACK_OVERFLOW, "traversal stack overflow");
+    if (bits & KERR_TIMEOUT) return fail(ctx, RT_ERR_TIMEOUT, "device wait timed out");
+    return fail(ctx, RT_ERR_INTERNAL, "kernel error bits 0x%x", bits);
+  }
+  return RT_SUCCESS;
+}
+
+rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, void *stream) {
+  if (!ctx || (n_jobs && !jobs)) return RT_ERR_INVALID_ARGUMENT;
+  for (uint32_t j = 0; j < n_jobs; j++) {
+    rt_status s = rtSetCamera(ctx, jobs[j].scene, &jobs[j].camera);
+    if (s != RT_SUCCESS) return s;
+    s = rtRender(ctx, jobs[j].scene, &jobs[j].params, jobs[j].d_rgba32f, stream);
+    if (s != RT_SUCCESS) return s;
+  }
+  return RT_SUCCESS;
+}
+
+}  // extern "C"

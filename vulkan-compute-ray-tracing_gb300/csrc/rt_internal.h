@@ -1,0 +1,94 @@
+// Internal declarations shared by the host runtime (api.cpp) and the kernel
+// translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rtgb/rt_api.h"
+#include "rtgb/rt_types.h"
+
+namespace rtgb {
+
+// Error bits kernels record in the context's device error word.
+enum : uint32_t {
+  KERR_STACK_OVERFLOW = 1u,
+  KERR_BAD_INDEX = 2u,
+  KERR_TIMEOUT = 4u,
+};
+
+// Device-resident scene, as the kernels see it.
+//
+// Reference layout (kept for parity downloads, light sampling and materials):
+//   tris    rt_triangle[ntris]   48 B
+//   nodes   rt_bvh_node[nnodes]  48 B, nnodes = 2*ntris - 1
+// Traversal layout (derived on the GPU from `nodes`):
+//   bvh2    4 x float4 per inner node (64 B): the boxes of both children,
+//           x/y slabs of child 0 and child 1, then the z slabs of both,
+//           then (ref0, ref1). ref >= 0 is an inner node, ref < 0 is the
+//           leaf ~k whose triangle is tpre[k].
+//   tpre    3 x float4 per triangle in leaf order (48 B): v0, n = cross(b, a),
+//           a = v0 - v1, b = v2 - v0 — the per-triangle terms of triIntersect
+//           (ray-trace-compute.comp:157-173), computed once with the same
+//           rounding.
+//   leaf_tri  original triangle index of leaf k.
+struct DevScene {
+  const rt_triangle *tris;
+  const rt_material *mats;
+  const rt_light *lights;
+  const rt_sphere *spheres;
+  const rt_bvh_node *nodes;
+  const float4 *bvh2;
+  const float4 *tpre;
+  const int32_t *leaf_tri;
+  float root_lo[3];
+  float root_hi[3];
+  int32_t root_ref;
+  uint32_t ntris, nmats, nlights, nspheres, nnodes;
+  uint32_t depth;
+};
+
+// ---------------------------------------------------------------- relayout.cu
+// Exclusive scan of n words (in may equal out); `sums` needs ceil(n/1024).
+cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t *sums, uint32_t n, cudaStream_t st);
+// Derives bvh2 / tpre / leaf_tri from the reference node array. `scratch`
+// holds 2*nnodes uint32 words.
+cudaError_t launch_relayout(const rt_bvh_node *nodes, uint32_t nnodes, const rt_triangle *tris, float4 *bvh2,
+                            float4 *tpre, int32_t *leaf_tri, uint32_t *scratch, cudaStream_t st);
+
+// ---------------------------------------------------------------- trace.cu
+// `counter` is a device word private to this launch (work distribution).
+cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
+                         uint32_t *err, cudaStream_t st);
+// The shader-literal 16-entry-stack traversal over the Bvh.h node array.
+cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
+                                   cudaStream_t st);
+
+// ---------------------------------------------------------------- render.cu
+// `segments` (may be NULL) accumulates the number of traced ray segments.
+cudaError_t launch_render(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
+                          unsigned long long *segments, uint32_t *err, cudaStream_t st);
+
+struct BatchJob {
+  DevScene sc;
+  rt_camera cam;
+  rt_render_params p;
+  float *accum;
+  uint32_t tile_begin;  // first tile of this job in the batch's tile space
+  uint32_t tiles_x;     // tiles per row
+};
+cudaError_t launch_render_batch(const BatchJob *d_jobs, uint32_t n_jobs, uint32_t total_tiles,
+                                const uint32_t *d_tile_job, uint32_t *d_counter, uint32_t *err,
+                                cudaStream_t st);
+
+// ---------------------------------------------------------------- bvh_build.cu
+// Builds the Bvh.h node array on the GPU. `axes` holds rand() % 3 for every
+// node in pop order (2*n - 1 values, host-generated from glibc's rand()).
+rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_axes, rt_bvh_node *d_nodes,
+                        cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen);
+
+// ---------------------------------------------------------------- glibc_rand.cpp
+// glibc's TYPE_3 random() (what rand() returns) after srand(seed).
+void glibc_rand_axes(uint32_t seed, uint64_t count, uint8_t *out_mod3);
+void glibc_rand_values(uint32_t seed, uint64_t count, int32_t *out);
+
+}  // namespace rtgb
