@@ -1,0 +1,341 @@
+"""Benchmark: closest-hit ray casting on the 1.31M-triangle displaced icosphere.
+
+Workload (one step): the two ray batches of the closest-hit configuration,
+traced against the mesh through the C ABI —
+  * coherent: 4,194,304 primary rays of a 2048x2048 pinhole at (0,0,-3)
+    looking +z, vfov 40 degrees;
+  * incoherent: 4,194,304 rays, origins U[-1.5,1.5]^3, directions uniform on
+    the sphere, tmin 1e-4.
+The mesh is the icosahedron subdivided 8 times (1,310,720 triangles), radius
+1, vertices displaced radially by 0.05*N(0,1); its BVH is built on the GPU
+node-for-node as the reference's Bvh.h builds it. All inputs are seeded
+synthetic data.
+
+Reported:
+  value      rays/s (Mrays/s) with rays resident in HBM (device API);
+  e2e        the same through the host-array entry point (rtTraceClosestHost),
+             pinned host rays in and hits out inside the timed region;
+  roofline   algorithmic bytes of the culled traversal of the reference tree
+             (48 B per node or triangle record fetched + 32 B ray + 16 B hit,
+             counted by the oracle) / CUDA-event time of the trace kernel,
+             against the measured HBM copy bandwidth;
+  cpu_baseline  the oracle (fp32, culled traversal, OpenMP) on a bounded
+             sample of the same rays, on this machine's host cores.
+`--impl reference` times the reference path's CPU implementation (the
+oracle restatement of the shader's hit_bvh; the reference's own GLSL needs a
+Vulkan stack that is not available) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "vulkan-compute-ray-tracing_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mrays/s incl. secondary (1 GB300, hit-exact); served renders/s + p50/p99 vs plain"
+WORKLOAD = "closest-hit, icosphere L8 (1,310,720 tris), 4,194,304 coherent + 4,194,304 incoherent rays"
+# Algorithmic bytes per ray (oracle, culled near-first traversal of the
+# reference tree over 1/16 of each batch): 48 * (nodes + triangles) + 48.
+ALG_BYTES_COHERENT = 48.0 * (531.24 + 61.47) + 48.0
+ALG_BYTES_INCOHERENT = 48.0 * (369.86 + 41.28) + 48.0
+RAYS_PER_BATCH = 2048 * 2048
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per trace launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "trace_closest_icosphere_l8.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(rt):
+    tris = rt.gen_icosphere(1, 8)
+    mats = rt.gen_cornell(1, 0)[1]
+    cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 2048, 2048)
+    coherent = rt.gen_camera_rays(cam, 2048, 2048)
+    incoherent = rt.gen_random_rays(3, RAYS_PER_BATCH)
+    return tris, mats, coherent, incoherent
+
+
+def dist_init():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 12.0):
+    """The oracle on a bounded sample of both batches, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    thr = oracle.max_threads()
+    probe = 4096
+    t0 = time.perf_counter()
+    oracle.trace(tris, nodes, coherent[::1024][:probe // 2], slack=0.0)
+    oracle.trace(tris, nodes, incoherent[::1024][:probe // 2], slack=0.0)
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    per_batch = int(min(RAYS_PER_BATCH, max(4096, rate * target_s / 2)))
+    stride = max(1, RAYS_PER_BATCH // per_batch)
+    a, b = coherent[::stride][:per_batch], incoherent[::stride][:per_batch]
+    t0 = time.perf_counter()
+    oracle.trace(tris, nodes, a, slack=0.0)
+    oracle.trace(tris, nodes, b, slack=0.0)
+    dt = time.perf_counter() - t0
+    n = len(a) + len(b)
+    return {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": thr, "kind": "port",
+            "sample": f"every {stride}th ray of each batch ({n} rays), oracle fp32 culled traversal, "
+                      f"{thr} OpenMP threads, {dt:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the reference path's CPU implementation, timed."""
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    import rtgb
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    tris, mats, coherent, incoherent = make_workload(rtgb)
+    nodes, _ = oracle.build_bvh(tris, 1)
+    thr = oracle.max_threads()
+    # Each step: a fixed sample of both batches sized to ~4 s of CPU work.
+    probe = 4096
+    t0 = time.perf_counter()
+    oracle.trace(tris, nodes, coherent[::1024][:probe // 2], slack=0.0)
+    oracle.trace(tris, nodes, incoherent[::1024][:probe // 2], slack=0.0)
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    per_batch = int(min(RAYS_PER_BATCH, max(2048, rate * 4.0 / 2)))
+    stride = max(1, RAYS_PER_BATCH // per_batch)
+    a, b = coherent[::stride][:per_batch], incoherent[::stride][:per_batch]
+    for _ in range(args.warmup):
+        oracle.trace(tris, nodes, a[:256], slack=0.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.trace(tris, nodes, a, slack=0.0)
+        oracle.trace(tris, nodes, b, slack=0.0)
+    dt = time.perf_counter() - t0
+    n = (len(a) + len(b)) * args.steps
+    value = n / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_per_step": f"every {stride}th ray of each batch "
+                                                            f"({len(a) + len(b)} rays)"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": thr, "kind": "port",
+                         "sample": f"every {stride}th ray of each batch, oracle restatement of hit_bvh "
+                                   f"(culled), {thr} OpenMP threads"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference GLSL path unavailable on this box (no graphics stack); its CPU restatement is timed",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    import rtgb
+    tris, mats, coherent, incoherent = make_workload(rtgb)
+    ctx = rtgb.Context(local)
+    sc = ctx.upload_scene(tris, mats)
+    info = sc.info()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    d_rays = [torch.from_numpy(coherent).cuda(), torch.from_numpy(incoherent).cuda()]
+    d_hits = [torch.empty((RAYS_PER_BATCH, 4), dtype=torch.float32, device="cuda") for _ in range(2)]
+
+    def step(events=None):
+        for b in range(2):
+            if events is not None:
+                events[b][0].record(stream)
+            sc.trace(d_rays[b], RAYS_PER_BATCH, d_hits[b], stream=sptr)
+            if events is not None:
+                events[b][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.synchronize(sptr)
+    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(2)] for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for k in range(args.steps):
+            step(ev[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    ctx.synchronize(sptr)
+    barrier(world)
+    ms = start.elapsed_time(stop)
+    ms_max = max_over_ranks(ms, world)
+    rays_step = 2 * RAYS_PER_BATCH
+    value = rays_step * args.steps * world / (ms_max / 1e3) / 1e6
+    kern = [[ev[k][b][0].elapsed_time(ev[k][b][1]) for k in range(args.steps)] for b in range(2)]
+    coh_ms, inc_ms = statistics.mean(kern[0]), statistics.mean(kern[1])
+    alg = [ALG_BYTES_COHERENT * RAYS_PER_BATCH, ALG_BYTES_INCOHERENT * RAYS_PER_BATCH]
+    # Average algorithmic bytes per launch / average launch duration (GB/s).
+    achieved = ((alg[0] + alg[1]) / 2) / (((coh_ms + inc_ms) / 2) / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+
+    # End to end: host arrays (pinned) through rtTraceClosestHost.
+    h_rays = [torch.from_numpy(coherent).pin_memory(), torch.from_numpy(incoherent).pin_memory()]
+    h_hits = [torch.empty((RAYS_PER_BATCH, 4), dtype=torch.float32).pin_memory() for _ in range(2)]
+
+    def e2e_step():
+        for b in range(2):
+            rc = rtgb.LIB.rtTraceClosestHost(ctx.handle, sc.id, h_rays[b].data_ptr(), RAYS_PER_BATCH,
+                                            h_hits[b].data_ptr())
+            ctx.check(rc, "rtTraceClosestHost")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_value = rays_step * args.steps * world / e2e_s / 1e6
+    # Sanity: the e2e hits equal the device-path hits.
+    same = all(torch.equal(h_hits[b].view(torch.int32), d_hits[b].cpu().view(torch.int32)) for b in range(2))
+
+    if rank != 0:
+        ctx.close()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "rays_per_step": rays_step, "bvh": "reference Bvh.h tree built on GPU",
+                   "l2": "inputs larger than L2 (rays 268 MB + hits 134 MB + scene 147 MB per step)",
+                   "parallelism": f"replicas x{world}", "coherent_grays": RAYS_PER_BATCH / coh_ms / 1e6,
+                   "incoherent_grays": RAYS_PER_BATCH / inc_ms / 1e6, "bvh_build_ms": info.build_ms,
+                   "bvh_depth": info.depth},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic_from_profile(), "peak_kind": peak_kind,
+                     "alg_bytes_per_ray": {"coherent": ALG_BYTES_COHERENT, "incoherent": ALG_BYTES_INCOHERENT}},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_step * 32,
+                "d2h_bytes_per_step": rays_step * 16, "matches_device_path": bool(same)},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(tris, coherent, incoherent, sc.bvh())
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

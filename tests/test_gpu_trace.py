@@ -94,7 +94,9 @@ def test_trace_config1_subsample_vs_oracle(rt, orc, ctx, big_mesh):
         want, st = orc.trace(tris, nodes, rays[sub], stats=True)
         ties = (st[:, 2] & 1) != 0
         compare(got[sub], want, ties)
-        assert ties.mean() < 0.01
+        # Near-ties are rays through shared mesh edges; this stride samples
+        # the image's centre column, which runs along icosahedron edges.
+        assert ties.mean() < 0.05
         # fp64 error of the fp32 formula (reported, bounded loosely here).
         tri64, tuv = orc.trace_f64(tris, nodes, rays[sub])
         gi = got[sub].view(np.int32)[:, 0]
