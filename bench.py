@@ -160,7 +160,7 @@ def max_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
-def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 12.0):
+def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 30.0):
     """The oracle on a bounded sample of both batches, all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -236,7 +236,11 @@ def run_gpu(args):
     ctx = rtgb.Context(local)
     sc = ctx.upload_scene(tris, mats)
     info = sc.info()
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: every launch and every CUDA event of the timed
+    # region is on it (the legacy default stream would not order against the
+    # library's non-blocking streams).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
     d_rays = [torch.from_numpy(coherent).cuda(), torch.from_numpy(incoherent).cuda()]
     d_hits = [torch.empty((RAYS_PER_BATCH, 4), dtype=torch.float32, device="cuda") for _ in range(2)]

@@ -129,8 +129,11 @@ rt_status rtRender(rt_ctx *ctx, rt_scene_id scene, const rt_render_params *param
  * ray-trace-compute.comp:262-311 as a stand-alone query). Stream-ordered. */
 rt_status rtTraceClosest(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,
                          void *stream);
-/* rtTraceClosest with compatibility flags: RT_COMPAT_STACK16 replays the
- * shader's 16-entry stack (comp:262,280), including its silent truncation. */
+/* rtTraceClosest with flags: RT_COMPAT_STACK16 replays the shader's 16-entry
+ * stack (comp:262,280), including its silent truncation; RT_HIT_FP32 returns
+ * t, u, v exactly as the fp32 triIntersect computes them instead of the
+ * default fp64 re-evaluation of the winning triangle. The hit index is the
+ * same either way. */
 rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,
                            uint32_t flags, void *stream);
 /* The same with host arrays: copies in, traces and copies out in pipelined

@@ -133,7 +133,12 @@ enum {
   RT_COMPAT_UNORM8 = 1u << 4,
   /* Shade with the alternate shader's hemisphere scatter
    * (ray-trace-compute-simple.comp:62-68). */
-  RT_SHADE_SIMPLE = 1u << 5
+  RT_SHADE_SIMPLE = 1u << 5,
+  /* Closest-hit queries: report t, u, v exactly as the reference's fp32
+   * triIntersect computes them. By default the winning triangle (chosen with
+   * that fp32 arithmetic) is re-intersected in fp64 with the same formula and
+   * t, u, v are that result rounded to fp32. */
+  RT_HIT_FP32 = 1u << 6
 };
 
 /* Per-render parameters (the reference's UBO plus its compile-time knobs:

@@ -536,7 +536,8 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
   if (!ctx || (n && (!rays || !hits))) return RT_ERR_INVALID_ARGUMENT;
   if ((uintptr_t)rays % 16 || (uintptr_t)hits % 16)
     return fail(ctx, RT_ERR_INVALID_ARGUMENT, "ray and hit arrays must be 16-byte aligned");
-  if (flags & ~RT_COMPAT_STACK16) return fail(ctx, RT_ERR_INVALID_ARGUMENT, "unsupported trace flags");
+  if (flags & ~(uint32_t)(RT_COMPAT_STACK16 | RT_HIT_FP32))
+    return fail(ctx, RT_ERR_INVALID_ARGUMENT, "unsupported trace flags");
   DevScene d;
   {
     std::lock_guard<std::mutex> g(ctx->mu);
@@ -547,7 +548,8 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
   if (n == 0) return RT_SUCCESS;
   cudaStream_t st = pick_stream(ctx, stream);
   cudaError_t e = (flags & RT_COMPAT_STACK16) ? launch_trace_literal16(d, rays, n, hits, st)
-                                               : launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, st);
+                                               : launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err,
+                                                              (flags & RT_HIT_FP32) == 0, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
   return RT_SUCCESS;
 }
@@ -582,7 +584,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     rt_ray *dr = (rt_ray *)ctx->stage[s];
     rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
     CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
-    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, st), "trace launch");
+    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, st), "trace launch");
     CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
   }
   CK(cudaStreamSynchronize(ctx->aux[0]), "trace");

@@ -1,6 +1,12 @@
 // Closest-hit ray casting: one thread per ray, rays fetched by warps from a
 // global work counter (persistent launch sized to the SM count), so warps
 // that finish early pick up new rays instead of idling behind long ones.
+//
+// The hit is chosen with the reference's fp32 arithmetic (traverse.cuh).
+// Unless RT_HIT_FP32 is set, t, u, v of the chosen triangle are then
+// recomputed once in fp64 with the same triIntersect formula
+// (ray-trace-compute.comp:157-173) and rounded to fp32, which removes the
+// cancellation error the fp32 formula shows at grazing angles.
 #include <cuda_runtime.h>
 
 #include "rt_internal.h"
@@ -13,7 +19,35 @@ namespace {
 constexpr int kTraceBlock = 128;
 constexpr int kBatch = 32;  // rays a warp takes per fetch
 
-template <int STACK>
+struct d3 {
+  double x, y, z;
+};
+__device__ __forceinline__ d3 dsub(d3 a, d3 b) { return d3{__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ double ddot(d3 a, d3 b) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ d3 dcross(d3 a, d3 b) {
+  return d3{__dsub_rn(__dmul_rn(a.y, b.z), __dmul_rn(b.y, a.z)), __dsub_rn(__dmul_rn(a.z, b.x), __dmul_rn(b.z, a.x)),
+            __dsub_rn(__dmul_rn(a.x, b.y), __dmul_rn(b.x, a.y))};
+}
+
+// triIntersect in fp64 on the original vertices (fp32 inputs widened).
+__device__ __forceinline__ void refine_fp64(const rt_triangle *__restrict__ tris, int tri, f3 o, f3 d, float &t,
+                                            float &u, float &v) {
+  const float4 *T = reinterpret_cast<const float4 *>(tris + tri);
+  float4 a4 = __ldg(T), b4 = __ldg(T + 1), c4 = __ldg(T + 2);
+  d3 v0{a4.x, a4.y, a4.z}, v1{b4.x, b4.y, b4.z}, v2{c4.x, c4.y, c4.z};
+  d3 ro{o.x, o.y, o.z}, rd{d.x, d.y, d.z};
+  d3 a = dsub(v0, v1), b = dsub(v2, v0), p = dsub(v0, ro);
+  d3 n = dcross(b, a);
+  d3 q = dcross(p, rd);
+  double idet = __ddiv_rn(1.0, ddot(rd, n));
+  u = __double2float_rn(__dmul_rn(ddot(q, b), idet));
+  v = __double2float_rn(__dmul_rn(ddot(q, a), idet));
+  t = __double2float_rn(__dmul_rn(ddot(n, p), idet));
+}
+
+template <int STACK, bool REFINE>
 __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4 *__restrict__ rays, uint32_t n,
                                                        int4 *__restrict__ hits, uint32_t *__restrict__ counter,
                                                        uint32_t *err) {
@@ -26,12 +60,15 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
     uint32_t i = base + lane;
     if (i < n) {
       float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
-      TraceRay r = make_ray(mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), r0.w);
+      f3 o = mk3(r0.x, r0.y, r0.z), d = mk3(r1.x, r1.y, r1.z);
+      TraceRay r = make_ray(o, d, r0.w);
       float closest = r1.w, u = 0.0f, v = 0.0f;
       int k = traverse_closest<STACK>(sc, r, closest, u, v, err);
       int4 h;
       if (k >= 0) {
-        h = make_int4(__ldg(sc.leaf_tri + k), __float_as_int(closest), __float_as_int(u), __float_as_int(v));
+        int tri = __ldg(sc.leaf_tri + k);
+        if (REFINE) refine_fp64(sc.tris, tri, o, d, closest, u, v);
+        h = make_int4(tri, __float_as_int(closest), __float_as_int(u), __float_as_int(v));
       } else {
         h = make_int4(-1, 0, 0, 0);
       }
@@ -54,18 +91,24 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_literal16(DevScene sc, co
 
 int g_num_sms = 0;
 
-}  // namespace
-
-cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
-                                   cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_trace_literal16<<<(n + kTraceBlock - 1) / kTraceBlock, kTraceBlock, 0, st>>>(
-      sc, reinterpret_cast<const float4 *>(rays), n, reinterpret_cast<int4 *>(hits));
+template <int STACK, bool REFINE>
+cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
+                           uint32_t *err, cudaStream_t st) {
+  int blocks_per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<STACK, REFINE>, kTraceBlock, 0);
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  uint32_t want = (n + kTraceBlock - 1) / kTraceBlock;
+  uint32_t grid = (uint32_t)(g_num_sms * blocks_per_sm);
+  if (grid > want) grid = want;
+  k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
+                                                       reinterpret_cast<int4 *>(hits), counter, err);
   return cudaGetLastError();
 }
 
+}  // namespace
+
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                         uint32_t *err, cudaStream_t st) {
+                         uint32_t *err, bool refine, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -75,23 +118,18 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
   // The work counter is private to this launch; reset it in stream order.
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  int blocks_per_sm = 0;
-  if (sc.depth <= 32) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<32>, kTraceBlock, 0);
-  } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<64>, kTraceBlock, 0);
-  }
-  if (blocks_per_sm < 1) blocks_per_sm = 1;
-  uint32_t want = (n + kTraceBlock - 1) / kTraceBlock;
-  uint32_t grid = (uint32_t)(g_num_sms * blocks_per_sm);
-  if (grid > want) grid = want;
-  if (sc.depth <= 32) {
-    k_trace<32><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                              reinterpret_cast<int4 *>(hits), counter, err);
-  } else {
-    k_trace<64><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                              reinterpret_cast<int4 *>(hits), counter, err);
-  }
+  if (sc.depth <= 32)
+    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, st)
+                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, st);
+  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, st)
+                : launch_variant<64, false>(sc, rays, n, hits, counter, err, st);
+}
+
+cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
+                                   cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_trace_literal16<<<(n + kTraceBlock - 1) / kTraceBlock, kTraceBlock, 0, st>>>(
+      sc, reinterpret_cast<const float4 *>(rays), n, reinterpret_cast<int4 *>(hits));
   return cudaGetLastError();
 }
 

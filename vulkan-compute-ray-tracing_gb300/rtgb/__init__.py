@@ -40,6 +40,7 @@ COMPAT_SPHERE_OVERRIDE = 1 << 2
 COMPAT_NO_SPHERES = 1 << 3
 COMPAT_UNORM8 = 1 << 4
 SHADE_SIMPLE = 1 << 5
+HIT_FP32 = 1 << 6
 
 STATUS = {0: "RT_SUCCESS", 1: "RT_ERR_INVALID_ARGUMENT", 2: "RT_ERR_OUT_OF_MEMORY", 3: "RT_ERR_CUDA",
           4: "RT_ERR_NOT_FOUND", 5: "RT_ERR_INVALID_SCENE", 6: "RT_ERR_STACK_OVERFLOW", 7: "RT_ERR_TIMEOUT",
