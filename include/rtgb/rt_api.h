@@ -141,6 +141,15 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays,
  * asynchronous DMA. */
 rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_rays, uint32_t n, rt_hit *h_hits);
 
+/* Launch-shape knobs of the context (the reference fixes its launch at
+ * compile time: local size 32x32, comp:3). Keys:
+ *   "trace.refill"  idle lanes of a warp that trigger a fetch of new rays
+ *                   in closest-hit casting (1..32; 32 = refill whole warps)
+ * Values persist for the context; the autotuner (rtgb.autotune) writes
+ * them. Unknown keys return RT_ERR_INVALID_ARGUMENT. */
+rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);
+rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value);
+
 /* Waits for the stream (NULL: the context stream) and reports any error a
  * kernel recorded since the last call (e.g. RT_ERR_STACK_OVERFLOW). */
 rt_status rtSynchronize(rt_ctx *ctx, void *stream);

@@ -124,9 +124,11 @@ def test_trace_config1_subsample_vs_oracle(rt, orc, ctx, big_mesh):
         # The fp32 formula itself (RT_HIT_FP32) is bit-exact with the fp32 oracle.
         raw = gpu_trace(ctx, sc, rays[sub], flags=rt.HIT_FP32)
         compare(raw, want, ties)
-        # Size-independent property over the full batch: a hit's t is in range.
+        # Size-independent property over the full batch: a hit's t is in range
+        # (the fp32 t passed tmin < t < tmax; the fp64 value may sit a few
+        # ulps lower at grazing hits right at tmin).
         hit = got.view(np.int32)[:, 0] >= 0
-        assert (got[hit, 1] > 1e-4).all() and (got[hit, 1] < 1e4).all()
+        assert (got[hit, 1] > 0.999e-4).all() and (got[hit, 1] < 1e4).all()
 
 
 def test_trace_handles_ragged_and_empty_batches(rt, orc, ctx):
@@ -197,3 +199,30 @@ def test_invalid_scenes_are_rejected(rt, ctx):
     # The context stays usable.
     sc = ctx.upload_scene(t, m)
     sc.release()
+
+
+@pytest.mark.parametrize("refill", [1, 4, 16, 32])
+def test_trace_refill_variants_agree(rt, ctx, refill):
+    """Every launch shape of the caster returns the same bits."""
+    tris, sc = mesh_scene(rt, ctx, 6, 7)
+    try:
+        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 128, 96)
+        rays = np.concatenate([rt.gen_camera_rays(cam, 128, 96), rt.gen_random_rays(11, 20000)])
+        base = gpu_trace(ctx, sc, rays)
+        old = ctx.get_tuning("trace.refill")
+        ctx.set_tuning("trace.refill", refill)
+        try:
+            got = gpu_trace(ctx, sc, rays)
+        finally:
+            ctx.set_tuning("trace.refill", old)
+        assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
+    finally:
+        sc.release()
+
+
+def test_tuning_keys(rt, ctx):
+    with pytest.raises(rt.RtError):
+        ctx.set_tuning("no.such.key", 1)
+    with pytest.raises(rt.RtError):
+        ctx.set_tuning("trace.refill", 0)
+    assert 1 <= ctx.get_tuning("trace.refill") <= 32

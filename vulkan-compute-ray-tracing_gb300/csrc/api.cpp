@@ -49,6 +49,7 @@ struct rt_ctx {
   uint32_t *d_counters = nullptr;  // kCounterRing launch-private work counters
   unsigned long long *d_segments = nullptr;
   std::atomic<uint32_t> counter_slot{0};
+  TraceOpts trace_opts;
   uint64_t budget = 0, used = 0, tick = 0;
   // Device staging for rtTraceClosestHost (two chunk buffers per aux stream).
   void *stage[2] = {nullptr, nullptr};
@@ -549,7 +550,7 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
   cudaStream_t st = pick_stream(ctx, stream);
   cudaError_t e = (flags & RT_COMPAT_STACK16) ? launch_trace_literal16(d, rays, n, hits, st)
                                                : launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err,
-                                                              (flags & RT_HIT_FP32) == 0, st);
+                                                              (flags & RT_HIT_FP32) == 0, ctx->trace_opts, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
   return RT_SUCCESS;
 }
@@ -584,7 +585,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     rt_ray *dr = (rt_ray *)ctx->stage[s];
     rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
     CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
-    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, st), "trace launch");
+    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, ctx->trace_opts, st), "trace launch");
     CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
   }
   CK(cudaStreamSynchronize(ctx->aux[0]), "trace");
@@ -625,6 +626,30 @@ rt_status rtReadSegmentCounter(rt_ctx *ctx, uint64_t *out, int reset) {
   if (reset) CK(cudaMemset(ctx->d_segments, 0, sizeof(v)), "reset counter");
   *out = v;
   return RT_SUCCESS;
+}
+
+rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
+  if (!ctx || !key) return RT_ERR_INVALID_ARGUMENT;
+  std::string k(key);
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (k == "trace.refill") {
+    if (value < 1 || value > 32) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.refill = (int)value;
+    return RT_SUCCESS;
+  }
+  ctx->last_error = "rtSetTuning: unknown key " + k;
+  return RT_ERR_INVALID_ARGUMENT;
+}
+
+rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
+  if (!ctx || !key || !value) return RT_ERR_INVALID_ARGUMENT;
+  std::string k(key);
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (k == "trace.refill") {
+    *value = ctx->trace_opts.refill;
+    return RT_SUCCESS;
+  }
+  return RT_ERR_INVALID_ARGUMENT;
 }
 
 rt_status rtSynchronize(rt_ctx *ctx, void *stream) {

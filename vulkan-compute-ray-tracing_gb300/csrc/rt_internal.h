@@ -56,10 +56,15 @@ cudaError_t launch_relayout(const rt_bvh_node *nodes, uint32_t nnodes, const rt_
                             float4 *tpre, int32_t *leaf_tri, uint32_t *scratch, cudaStream_t st);
 
 // ---------------------------------------------------------------- trace.cu
+// Launch-shape knobs of closest-hit casting (rtSetTuning).
+struct TraceOpts {
+  int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
+};
+
 // `counter` is a device word private to this launch (work distribution);
 // `refine` recomputes t, u, v of the winning triangle in fp64.
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                         uint32_t *err, bool refine, cudaStream_t st);
+                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st);
 // The shader-literal 16-entry-stack traversal over the Bvh.h node array.
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
                                    cudaStream_t st);

@@ -9,6 +9,8 @@
 // cancellation error the fp32 formula shows at grazing angles.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "rt_internal.h"
 #include "shade.cuh"
 #include "traverse.cuh"
@@ -17,7 +19,7 @@ namespace rtgb {
 namespace {
 
 constexpr int kTraceBlock = 128;
-constexpr int kBatch = 32;  // rays a warp takes per fetch
+
 
 struct d3 {
   double x, y, z;
@@ -47,14 +49,117 @@ __device__ __forceinline__ void refine_fp64(const rt_triangle *__restrict__ tris
   t = __double2float_rn(__dmul_rn(ddot(n, p), idet));
 }
 
+constexpr int kDone = INT_MIN;  // no node left: the ray is finished
+
+// Persistent warps with per-lane refill: each lane owns one ray at a time;
+// when at least `refill` lanes of a warp have finished, the warp claims that
+// many new rays with one atomic and the idle lanes start on them, so a warp
+// never waits for its slowest ray with most lanes idle. Traversal runs as
+// while-while: descend inner nodes until every active lane holds a leaf,
+// then test those triangles together.
 template <int STACK, bool REFINE>
 __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4 *__restrict__ rays, uint32_t n,
                                                        int4 *__restrict__ hits, uint32_t *__restrict__ counter,
-                                                       uint32_t *err) {
+                                                       uint32_t *err, int refill) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const float4 *__restrict__ bvh = sc.bvh2;
+  int stack[STACK];
+  int sp = 0, node = kDone, best = -1;
+  int64_t ray_id = -1;
+  float closest = 0.0f, bu = 0.0f, bv = 0.0f;
+  TraceRay r;
+  r.tmin = 0.0f;
+  bool exhausted = false;
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xffffffffu, ray_id < 0);
+    if (!exhausted && __popc(idle) >= refill) {
+      const uint32_t cnt = __popc(idle);
+      const uint32_t leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(counter, cnt);
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + cnt >= n) exhausted = true;
+      if (ray_id < 0) {
+        uint32_t my = base + __popc(idle & lt_mask);
+        if (my < n) {
+          float4 r0 = __ldg(rays + 2ull * my), r1 = __ldg(rays + 2ull * my + 1);
+          r = make_ray(mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), r0.w);
+          closest = r1.w;
+          best = -1;
+          sp = 0;
+          ray_id = my;
+          float root = slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1], sc.root_lo[2],
+                                  sc.root_hi[2], closest);
+          node = root < __int_as_float(0x7f800000) ? sc.root_ref : kDone;
+        }
+      }
+    }
+    // Leave only when no lane holds a ray after this round's fetch.
+    if (exhausted && __all_sync(0xffffffffu, ray_id < 0)) return;
+    if (ray_id >= 0) {
+      // Inner nodes until this lane holds a leaf or runs out of work.
+      while (node >= 0) {
+        const float4 *N = bvh + 4ll * node;
+        float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
+        float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+        float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+        int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+        bool h0 = t0 < __int_as_float(0x7f800000), h1 = t1 < __int_as_float(0x7f800000);
+        if (h0 && h1) {
+          int nearc = r0, farc = r1;
+          if (t1 < t0) {
+            nearc = r1;
+            farc = r0;
+          }
+          if (sp >= STACK) {
+            atomicOr(err, KERR_STACK_OVERFLOW);
+            node = kDone;
+            break;
+          }
+          stack[sp++] = farc;
+          node = nearc;
+        } else if (h0) {
+          node = r0;
+        } else if (h1) {
+          node = r1;
+        } else {
+          node = sp > 0 ? stack[--sp] : kDone;
+        }
+      }
+      if (node != kDone) {
+        test_triangle(sc.tpre, ~node, r, closest, best, bu, bv);
+        node = sp > 0 ? stack[--sp] : kDone;
+      }
+      if (node == kDone) {
+        int4 h;
+        if (best >= 0) {
+          int tri = __ldg(sc.leaf_tri + best);
+          float t = closest, u = bu, v = bv;
+          if (REFINE) refine_fp64(sc.tris, tri, r.o, r.d, t, u, v);
+          h = make_int4(tri, __float_as_int(t), __float_as_int(u), __float_as_int(v));
+        } else {
+          h = make_int4(-1, 0, 0, 0);
+        }
+        hits[ray_id] = h;
+        ray_id = -1;
+      }
+    }
+  }
+}
+
+// Whole-warp batches: a warp claims 32 consecutive rays and each lane runs
+// its ray to completion in a tight loop. Consecutive rays of a camera are
+// neighbours on screen, so the lanes of a warp walk similar parts of the
+// tree; this is the faster form for coherent batches.
+template <int STACK, bool REFINE>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_batch(DevScene sc, const float4 *__restrict__ rays,
+                                                             uint32_t n, int4 *__restrict__ hits,
+                                                             uint32_t *__restrict__ counter, uint32_t *err) {
   const uint32_t lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(counter, kBatch);
+    if (lane == 0) base = atomicAdd(counter, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) return;
     uint32_t i = base + lane;
@@ -93,22 +198,30 @@ int g_num_sms = 0;
 
 template <int STACK, bool REFINE>
 cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                           uint32_t *err, cudaStream_t st) {
+                           uint32_t *err, const TraceOpts &opts, cudaStream_t st) {
+  const bool batch = opts.refill >= 32;
   int blocks_per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<STACK, REFINE>, kTraceBlock, 0);
+  if (batch)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_batch<STACK, REFINE>, kTraceBlock, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<STACK, REFINE>, kTraceBlock, 0);
   if (blocks_per_sm < 1) blocks_per_sm = 1;
   uint32_t want = (n + kTraceBlock - 1) / kTraceBlock;
   uint32_t grid = (uint32_t)(g_num_sms * blocks_per_sm);
   if (grid > want) grid = want;
-  k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                       reinterpret_cast<int4 *>(hits), counter, err);
+  if (batch)
+    k_trace_batch<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
+                                                               reinterpret_cast<int4 *>(hits), counter, err);
+  else
+    k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
+                                                         reinterpret_cast<int4 *>(hits), counter, err, opts.refill);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                         uint32_t *err, bool refine, cudaStream_t st) {
+                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -119,10 +232,10 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (sc.depth <= 32)
-    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, st)
-                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, st);
-  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, st)
-                : launch_variant<64, false>(sc, rays, n, hits, counter, err, st);
+    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, opts, st)
+                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, opts, st);
+  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, opts, st)
+                : launch_variant<64, false>(sc, rays, n, hits, counter, err, opts, st);
 }
 
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,

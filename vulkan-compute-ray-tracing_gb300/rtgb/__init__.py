@@ -110,6 +110,8 @@ def _load() -> ctypes.CDLL:
         "rtTraceClosestEx": (I32, [P, U32, P, U32, P, U32, P]),
         "rtTraceClosestHost": (I32, [P, U32, P, U32, P]),
         "rtSynchronize": (I32, [P, P]),
+        "rtSetTuning": (I32, [P, ctypes.c_char_p, ctypes.c_int64]),
+        "rtGetTuning": (I32, [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),
         "rtReadSegmentCounter": (I32, [P, ctypes.POINTER(U64), I32]),
         "rtRenderBatch": (I32, [P, ctypes.POINTER(RenderJob), U32, P]),
         "rtgbGenCornell": (U32, [U64, U32, U32, F32, F32, F32, P, P, P]),
@@ -270,6 +272,14 @@ class Context:
                                _ptr(spheres), 0 if spheres is None else len(spheres), bvh_seed, ctypes.byref(sid))
         self.check(st, "rtUploadScene")
         return Scene(self, sid.value)
+
+    def set_tuning(self, key: str, value: int):
+        self.check(LIB.rtSetTuning(self.handle, key.encode(), int(value)), "rtSetTuning")
+
+    def get_tuning(self, key: str) -> int:
+        v = ctypes.c_int64()
+        self.check(LIB.rtGetTuning(self.handle, key.encode(), ctypes.byref(v)), "rtGetTuning")
+        return v.value
 
     def synchronize(self, stream=None):
         self.check(LIB.rtSynchronize(self.handle, stream), "rtSynchronize")
