@@ -160,6 +160,26 @@ rt_status rtSynchronize(rt_ctx *ctx, void *stream);
  * counter. */
 rt_status rtReadSegmentCounter(rt_ctx *ctx, uint64_t *out, int reset);
 
+/* Allocation-free BVH build. No counterpart in the reference (which builds
+ * its tree on the CPU); this is the same GPU build rtUploadScene runs, for
+ * callers that may not allocate device memory — a host application whose
+ * device memory is owned by another allocator or runtime, or code running
+ * where cudaMalloc is forbidden. It allocates nothing: its scratch is a
+ * fixed array inside the library (about 3.9 MB on every GPU that loads the
+ * library, held until the process exits) plus static host buffers.
+ *   d_triangles  n triangles in device memory (Bvh.h layout, finite vertices)
+ *   n            1 .. 65536; larger n returns RT_ERR_INVALID_ARGUMENT
+ *   bvh_seed     the rand() seed, as in rtUploadScene (the reference: 1)
+ *   d_nodes      2n-1 nodes of device memory receiving the Bvh.h node array
+ *   stream       cudaStream_t (NULL: the legacy default stream)
+ * Returns once the nodes are written. The first call on a device looks up
+ * the array's device address (make it before any stream capture). Calls
+ * share the array: they are serialised inside the library, and work that
+ * overlaps a call on the same device from outside it races. Both pointers
+ * must be 16-byte aligned. */
+rt_status rtBuildBvhNoAlloc(const rt_triangle *d_triangles, uint32_t n, uint32_t bvh_seed, rt_bvh_node *d_nodes,
+                            void *stream);
+
 /* ------------------------------------------------------------------ batches
  * Many renders of uneven size in one launch. */
 typedef struct rt_render_job {

@@ -593,3 +593,153 @@ done:
 }
 
 }  // namespace rtgb
+
+// ---------------------------------------------------------------------------
+// Allocation-free build: rtBuildBvhNoAlloc.
+//
+// For callers that cannot allocate device memory, the same kernels run on a
+// fixed scratch area that is part of the library image: a file-scope
+// __device__ array sized for kNoAllocMaxTriangles triangles (about 3.9 MB,
+// held by every GPU that loads the library until the process exits). The
+// host-side bookkeeping uses static buffers as well, so a call performs no
+// allocation of any kind. All calls share both areas: calls must not
+// overlap (they are serialised on the host by a mutex and each call waits
+// for its own GPU work before returning; calls issued by other means on the
+// same device while one is running would race on the shared array).
+#include <mutex>
+
+namespace rtgb {
+namespace {
+
+constexpr uint32_t kNoAllocMaxTriangles = 65536;
+constexpr size_t kNaAlign(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kNaKey = 0;
+constexpr size_t kNaIdx = kNaKey + kNaAlign(4ull * kNoAllocMaxTriangles);
+constexpr size_t kNaP = kNaIdx + kNaAlign(4ull * kNoAllocMaxTriangles);
+constexpr size_t kNaQ = kNaP + kNaAlign(4ull * kNoAllocMaxTriangles);
+constexpr size_t kNaQueue = kNaQ + kNaAlign(4ull * kNoAllocMaxTriangles);
+constexpr size_t kNaSegs = kNaQueue + kNaAlign(sizeof(Range) * kNoAllocMaxTriangles);
+constexpr size_t kNaLeaves = kNaSegs + kNaAlign(sizeof(Seg) * kNoAllocMaxTriangles);
+constexpr size_t kNaCtr = kNaLeaves + kNaAlign(sizeof(Leaf) * kNoAllocMaxTriangles);
+constexpr size_t kNaBytes = kNaCtr + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NaItem {
+  uint32_t off, n, node;
+  uint64_t rank, leaves_before;
+};
+struct NaHost {
+  uint8_t axes[2 * kNoAllocMaxTriangles];
+  Seg segs[kNoAllocMaxTriangles];
+  Leaf leaves[kNoAllocMaxTriangles];
+  NaItem cur[kNoAllocMaxTriangles], next[kNoAllocMaxTriangles];
+  uint32_t level_off[72];
+  uint32_t levels, nsegs, nleaves;
+  uint32_t flags[4];
+};
+static NaHost g_na_host;
+static std::mutex g_na_mu;
+constexpr int kNaMaxDevices = 64;
+static unsigned char *g_na_dev[kNaMaxDevices];  // device address of the scratch array, per device
+
+// The topology replay of host_topology() written into the static buffers.
+void na_topology(uint32_t n, NaHost &h) {
+  uint32_t ncur = 1, nnext = 0;
+  h.cur[0] = NaItem{0, n, 0, 0, 0};
+  h.levels = 0;
+  h.nsegs = 0;
+  h.nleaves = 0;
+  while (ncur) {
+    h.level_off[h.levels++] = h.nsegs;
+    nnext = 0;
+    for (uint32_t i = 0; i < ncur; i++) {
+      const NaItem it = h.cur[i];
+      if (it.n <= 1) {
+        h.leaves[h.nleaves++] = Leaf{it.node, it.off};
+        continue;
+      }
+      uint32_t k = (uint32_t)(it.rank - it.leaves_before);
+      uint32_t nl = it.n / 2, nr = it.n - nl;
+      Seg s;
+      s.off = it.off;
+      s.n = it.n;
+      s.node = it.node;
+      s.kchild = k;
+      s.axis = h.axes[it.rank];
+      s.depth = 2u * (uint32_t)sortemu::floor_log2(it.n);
+      h.segs[h.nsegs++] = s;
+      h.next[nnext++] = NaItem{it.off, nl, 2 * k + 1, it.rank + 1 + (2ull * nr - 1), it.leaves_before + nr};
+      h.next[nnext++] = NaItem{it.off + nl, nr, 2 * k + 2, it.rank + 1, it.leaves_before};
+    }
+    for (uint32_t i = 0; i < nnext; i++) h.cur[i] = h.next[i];
+    ncur = nnext;
+  }
+  h.level_off[h.levels] = h.nsegs;
+}
+
+}  // namespace
+}  // namespace rtgb
+
+extern "C" rt_status rtBuildBvhNoAlloc(const rt_triangle *d_triangles, uint32_t n, uint32_t bvh_seed,
+                                       rt_bvh_node *d_nodes, void *stream) {
+  using namespace rtgb;
+  if (!d_triangles || !d_nodes || n == 0 || n > kNoAllocMaxTriangles) return RT_ERR_INVALID_ARGUMENT;
+  if ((uintptr_t)d_triangles % 16 || (uintptr_t)d_nodes % 16) return RT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> guard(g_na_mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return RT_ERR_CUDA;
+  if (!g_na_dev[dev]) {
+    // Once per device, with that device current: host code cannot use the
+    // array's name as a device address, so look the address up.
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return RT_ERR_CUDA;
+    g_na_dev[dev] = static_cast<unsigned char *>(p);
+  }
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return RT_ERR_CUDA;
+  unsigned char *base = g_na_dev[dev];
+  float *key = reinterpret_cast<float *>(base + kNaKey);
+  uint32_t *idx = reinterpret_cast<uint32_t *>(base + kNaIdx);
+  uint32_t *P = reinterpret_cast<uint32_t *>(base + kNaP);
+  uint32_t *Q = reinterpret_cast<uint32_t *>(base + kNaQ);
+  Range *queue = reinterpret_cast<Range *>(base + kNaQueue);
+  Seg *dsegs = reinterpret_cast<Seg *>(base + kNaSegs);
+  Leaf *dleaves = reinterpret_cast<Leaf *>(base + kNaLeaves);
+  uint32_t *ctr = reinterpret_cast<uint32_t *>(base + kNaCtr);
+
+  NaHost &h = g_na_host;
+  glibc_rand_axes(bvh_seed, 2ull * n - 1, h.axes);
+  na_topology(n, h);
+  if (h.nsegs &&
+      cudaMemcpyAsync(dsegs, h.segs, sizeof(Seg) * h.nsegs, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return RT_ERR_CUDA;
+  if (cudaMemcpyAsync(dleaves, h.leaves, sizeof(Leaf) * h.nleaves, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return RT_ERR_CUDA;
+  // The error word survives from earlier calls: clear it.
+  if (cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 4, st) != cudaSuccess) return RT_ERR_CUDA;
+  k_iota<<<(n + 255) / 256, 256, 0, st>>>(idx, n);
+  for (uint32_t L = 0; L < h.levels; L++) {
+    uint32_t s0 = h.level_off[L], s1 = h.level_off[L + 1];
+    uint32_t ns = s1 - s0;
+    if (ns == 0) continue;
+    const Seg *ls = dsegs + s0;
+    // Queue count and head start at zero for every level; keep the error word.
+    if (cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 2, st) != cudaSuccess) return RT_ERR_CUDA;
+    k_keys<<<(n + 255) / 256, 256, 0, st>>>(ls, ns, d_triangles, idx, key, n);
+    k_enqueue<<<(ns + 255) / 256, 256, 0, st>>>(ls, ns, queue, ctr);
+    uint32_t maxn = 0;
+    for (uint32_t j = s0; j < s1; j++) maxn = std::max(maxn, h.segs[j].n);
+    if (maxn > kWarpMax) k_sort_big<<<ns, kBigThreads, 0, st>>>(ls, key, idx, P, Q, queue, ctr, ctr + 2);
+    k_sort_warps<<<(uint32_t)sms * 8u, 256, 0, st>>>(key, idx, P, Q, queue, ctr, ctr + 1, ctr + 2);
+  }
+  k_leaves<<<(h.nleaves + 255) / 256, 256, 0, st>>>(dleaves, h.nleaves, idx, d_triangles, d_nodes);
+  for (int L = (int)h.levels - 1; L >= 0; L--) {
+    uint32_t s0 = h.level_off[L], s1 = h.level_off[L + 1];
+    if (s1 > s0) k_inner<<<(s1 - s0 + 255) / 256, 256, 0, st>>>(dsegs + s0, s1 - s0, d_nodes);
+  }
+  if (cudaGetLastError() != cudaSuccess) return RT_ERR_CUDA;
+  if (cudaMemcpyAsync(h.flags, ctr, sizeof(h.flags), cudaMemcpyDeviceToHost, st) != cudaSuccess) return RT_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return RT_ERR_CUDA;
+  return h.flags[2] ? RT_ERR_INTERNAL : RT_SUCCESS;
+}
