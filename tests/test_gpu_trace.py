@@ -201,21 +201,26 @@ def test_invalid_scenes_are_rejected(rt, ctx):
     sc.release()
 
 
-@pytest.mark.parametrize("refill", [1, 4, 16, 32])
-def test_trace_refill_variants_agree(rt, ctx, refill):
-    """Every launch shape of the caster returns the same bits."""
+@pytest.mark.parametrize("refill,sort", [(1, 0), (4, 0), (16, 0), (32, 0), (32, 1), (4, 1)])
+def test_trace_launch_shapes_agree(rt, ctx, refill, sort):
+    """Every launch shape of the caster (refill threshold, Morton order)
+    returns the same bits, in input order."""
     tris, sc = mesh_scene(rt, ctx, 6, 7)
     try:
-        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 128, 96)
-        rays = np.concatenate([rt.gen_camera_rays(cam, 128, 96), rt.gen_random_rays(11, 20000)])
+        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 256, 200)
+        rays = np.concatenate([rt.gen_camera_rays(cam, 256, 200), rt.gen_random_rays(11, 40000)])
         base = gpu_trace(ctx, sc, rays)
-        old = ctx.get_tuning("trace.refill")
+        old = (ctx.get_tuning("trace.refill"), ctx.get_tuning("trace.sort"))
         ctx.set_tuning("trace.refill", refill)
+        ctx.set_tuning("trace.sort", sort)
         try:
             got = gpu_trace(ctx, sc, rays)
+            host = sc.trace_host(rays)
         finally:
-            ctx.set_tuning("trace.refill", old)
+            ctx.set_tuning("trace.refill", old[0])
+            ctx.set_tuning("trace.sort", old[1])
         assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
+        assert np.array_equal(host.view(np.uint32), base.view(np.uint32))
     finally:
         sc.release()
 

@@ -548,9 +548,29 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
   }
   if (n == 0) return RT_SUCCESS;
   cudaStream_t st = pick_stream(ctx, stream);
-  cudaError_t e = (flags & RT_COMPAT_STACK16) ? launch_trace_literal16(d, rays, n, hits, st)
-                                               : launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err,
-                                                              (flags & RT_HIT_FP32) == 0, ctx->trace_opts, st);
+  TraceOpts opts;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    opts = ctx->trace_opts;
+  }
+  if (flags & RT_COMPAT_STACK16) {
+    cudaError_t e = launch_trace_literal16(d, rays, n, hits, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
+    return RT_SUCCESS;
+  }
+  const bool refine = (flags & RT_HIT_FP32) == 0;
+  if (opts.sort && n >= 65536) {
+    // Stream-ordered scratch from the device memory pool.
+    void *scratch = nullptr;
+    CK(cudaMallocAsync(&scratch, raysort_scratch_bytes(n), st), "ray sort scratch");
+    uint32_t *perm = nullptr;
+    cudaError_t e = launch_raysort(rays, n, scratch, &perm, st);
+    if (e == cudaSuccess) e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st, perm);
+    cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
+    return RT_SUCCESS;
+  }
+  cudaError_t e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
   return RT_SUCCESS;
 }
@@ -566,6 +586,11 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
   }
   if (n == 0) return RT_SUCCESS;
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  TraceOpts opts;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    opts = ctx->trace_opts;
+  }
   // Chunks alternate between two streams so the copy of one chunk overlaps
   // the traversal of the other.
   const uint32_t chunk = 1u << 20;
@@ -585,7 +610,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     rt_ray *dr = (rt_ray *)ctx->stage[s];
     rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
     CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
-    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, ctx->trace_opts, st), "trace launch");
+    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st), "trace launch");
     CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
   }
   CK(cudaStreamSynchronize(ctx->aux[0]), "trace");
@@ -637,6 +662,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.refill = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.sort") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.sort = (int)value;
+    return RT_SUCCESS;
+  }
   ctx->last_error = "rtSetTuning: unknown key " + k;
   return RT_ERR_INVALID_ARGUMENT;
 }
@@ -647,6 +677,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   std::lock_guard<std::mutex> g(ctx->mu);
   if (k == "trace.refill") {
     *value = ctx->trace_opts.refill;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.sort") {
+    *value = ctx->trace_opts.sort;
     return RT_SUCCESS;
   }
   return RT_ERR_INVALID_ARGUMENT;

@@ -59,12 +59,20 @@ cudaError_t launch_relayout(const rt_bvh_node *nodes, uint32_t nnodes, const rt_
 // Launch-shape knobs of closest-hit casting (rtSetTuning).
 struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
+  int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
 };
 
 // `counter` is a device word private to this launch (work distribution);
 // `refine` recomputes t, u, v of the winning triangle in fp64.
+// `perm` (may be NULL) gives the order rays are cast in; hits always land
+// at their ray's input index.
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st);
+                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st,
+                         const uint32_t *perm = nullptr);
+// Morton bucketing of a ray batch (raysort.cu); `scratch` holds
+// raysort_scratch_bytes(n); *perm_out points into it.
+size_t raysort_scratch_bytes(uint32_t n);
+cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, void *scratch, uint32_t **perm_out, cudaStream_t st);
 // The shader-literal 16-entry-stack traversal over the Bvh.h node array.
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
                                    cudaStream_t st);

@@ -60,7 +60,7 @@ constexpr int kDone = INT_MIN;  // no node left: the ray is finished
 template <int STACK, bool REFINE>
 __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4 *__restrict__ rays, uint32_t n,
                                                        int4 *__restrict__ hits, uint32_t *__restrict__ counter,
-                                                       uint32_t *err, int refill) {
+                                                       uint32_t *err, int refill, const uint32_t *__restrict__ perm) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const float4 *__restrict__ bvh = sc.bvh2;
@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
       if (ray_id < 0) {
         uint32_t my = base + __popc(idle & lt_mask);
         if (my < n) {
+          if (perm) my = __ldg(perm + my);
           float4 r0 = __ldg(rays + 2ull * my), r1 = __ldg(rays + 2ull * my + 1);
           r = make_ray(mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), r0.w);
           closest = r1.w;
@@ -155,7 +156,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
 template <int STACK, bool REFINE>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(DevScene sc, const float4 *__restrict__ rays,
                                                              uint32_t n, int4 *__restrict__ hits,
-                                                             uint32_t *__restrict__ counter, uint32_t *err) {
+                                                             uint32_t *__restrict__ counter, uint32_t *err,
+                                                             const uint32_t *__restrict__ perm) {
   const uint32_t lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -164,6 +166,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(DevScene sc, const 
     if (base >= n) return;
     uint32_t i = base + lane;
     if (i < n) {
+      if (perm) i = __ldg(perm + i);
       float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
       f3 o = mk3(r0.x, r0.y, r0.z), d = mk3(r1.x, r1.y, r1.z);
       TraceRay r = make_ray(o, d, r0.w);
@@ -198,7 +201,7 @@ int g_num_sms = 0;
 
 template <int STACK, bool REFINE>
 cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                           uint32_t *err, const TraceOpts &opts, cudaStream_t st) {
+                           uint32_t *err, const TraceOpts &opts, const uint32_t *perm, cudaStream_t st) {
   const bool batch = opts.refill >= 32;
   int blocks_per_sm = 0;
   if (batch)
@@ -211,17 +214,18 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
   if (grid > want) grid = want;
   if (batch)
     k_trace_batch<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                               reinterpret_cast<int4 *>(hits), counter, err);
+                                                               reinterpret_cast<int4 *>(hits), counter, err, perm);
   else
     k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                         reinterpret_cast<int4 *>(hits), counter, err, opts.refill);
+                                                         reinterpret_cast<int4 *>(hits), counter, err, opts.refill,
+                                                         perm);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st) {
+                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st, const uint32_t *perm) {
   if (n == 0) return cudaSuccess;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -232,10 +236,10 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (sc.depth <= 32)
-    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, opts, st)
-                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, opts, st);
-  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, opts, st)
-                : launch_variant<64, false>(sc, rays, n, hits, counter, err, opts, st);
+    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, opts, perm, st)
+                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, opts, perm, st);
+  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, opts, perm, st)
+                : launch_variant<64, false>(sc, rays, n, hits, counter, err, opts, perm, st);
 }
 
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
