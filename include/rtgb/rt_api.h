@@ -145,9 +145,14 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  * compile time: local size 32x32, comp:3). Keys:
  *   "trace.refill"  idle lanes of a warp that trigger a fetch of new rays
  *                   in closest-hit casting (1..32; 32 = refill whole warps)
- *   "trace.sort"    1 = cast batches of >= 65536 rays in Morton order of
- *                   origin and direction (hits still land at their ray's
- *                   input index; scratch comes from the stream-ordered pool)
+ *   "trace.sort"    1 (default) = cast batches of >= 65536 rays in Morton
+ *                   order of origin and direction (hits still land at their
+ *                   ray's input index; scratch comes from the stream-ordered
+ *                   pool); also reorders each bounce of a wavefront render
+ *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
+ *                   1 wavefront (per-bounce kernels over compacted queues),
+ *                   2 (default) wavefront from 1024x1024 pixels up; images are
+ *                   identical in every mode
  * Values persist for the context; the autotuner (rtgb.autotune) writes
  * them. Unknown keys return RT_ERR_INVALID_ARGUMENT. */
 rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);

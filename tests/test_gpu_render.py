@@ -122,3 +122,46 @@ def test_render_without_camera_is_an_error(rt, ctx):
             sc.render(accum, 8, 8)
     finally:
         sc.release()
+
+
+@pytest.mark.parametrize("flags,spheres,spp", [(0, 6, 3), ("LEN1", 6, 2), ("SPHERE_OVERRIDE", 6, 1),
+                                               ("NO_SPHERES", 0, 2), ("UNORM8", 3, 3), ("SHADE_SIMPLE", 3, 1)])
+def test_wavefront_equals_megakernel(rt, ctx, flags, spheres, spp):
+    """The wavefront split (with per-bounce Morton reordering) gives the
+    megakernel's image bit for bit, and counts the same segments."""
+    import torch
+    f = 0 if flags == 0 else (getattr(rt, "COMPAT_" + flags, None) or getattr(rt, flags))
+    t, m, s, sc = cornell(rt, ctx, n_soup=5000, n_spheres=spheres, seed=6)
+    try:
+        W, H = 160, 120
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
+        out = {}
+        old = ctx.get_tuning("render.mode")
+        try:
+            for mode in (0, 1):
+                ctx.set_tuning("render.mode", mode)
+                ctx.segments(reset=True)
+                out[mode] = (gpu_render(sc, cam, W, H, spp=spp, max_bounces=7, sample_index=2, flags=f),
+                             ctx.segments(reset=True))
+        finally:
+            ctx.set_tuning("render.mode", old)
+        assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+        assert out[0][1] == out[1][1]
+    finally:
+        sc.release()
+
+
+def test_wavefront_config0_vs_oracle(rt, orc, ctx):
+    t, m, s, sc = cornell(rt, ctx, n_spheres=4)
+    try:
+        old = ctx.get_tuning("render.mode")
+        ctx.set_tuning("render.mode", 1)
+        try:
+            cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 256, 256)
+            img = gpu_render(sc, cam, 256, 256, spp=1, max_bounces=8)
+        finally:
+            ctx.set_tuning("render.mode", old)
+        want, _ = orc.render(t, m, sc.bvh(), sc.lights(), s, cam.as_array(), 256, 256, spp=1, max_bounces=8)
+        assert (mae(img, want) <= TOL).all()
+    finally:
+        sc.release()

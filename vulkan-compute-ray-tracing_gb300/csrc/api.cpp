@@ -50,6 +50,7 @@ struct rt_ctx {
   unsigned long long *d_segments = nullptr;
   std::atomic<uint32_t> counter_slot{0};
   TraceOpts trace_opts;
+  RenderOpts render_opts;
   uint64_t budget = 0, used = 0, tick = 0;
   // Device staging for rtTraceClosestHost (two chunk buffers per aux stream).
   void *stage[2] = {nullptr, nullptr};
@@ -564,7 +565,7 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
     void *scratch = nullptr;
     CK(cudaMallocAsync(&scratch, raysort_scratch_bytes(n), st), "ray sort scratch");
     uint32_t *perm = nullptr;
-    cudaError_t e = launch_raysort(rays, n, scratch, &perm, st);
+    cudaError_t e = launch_raysort(rays, n, nullptr, scratch, &perm, st);
     if (e == cudaSuccess) e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st, perm);
     cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
@@ -636,7 +637,27 @@ rt_status rtRender(rt_ctx *ctx, rt_scene_id id, const rt_render_params *p, float
     d = sc->dev;
     cam = sc->camera;
   }
-  cudaError_t e = launch_render(d, cam, *p, accum, ctx->d_segments, ctx->d_err, pick_stream(ctx, stream));
+  cudaStream_t st = pick_stream(ctx, stream);
+  RenderOpts ropts;
+  TraceOpts topts;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ropts = ctx->render_opts;
+    topts = ctx->trace_opts;
+  }
+  const uint64_t pixels = (uint64_t)p->width * p->height;
+  bool wavefront = ropts.mode == 1 || (ropts.mode == 2 && pixels >= (1u << 20));
+  if (p->flags & RT_COMPAT_STACK16) wavefront = false;  // the literal 16-entry traversal runs in the megakernel
+  if (wavefront && pixels < (1ull << 31)) {
+    void *scratch = nullptr;
+    CK(cudaMallocAsync(&scratch, wavefront_scratch_bytes((uint32_t)pixels), st), "wavefront scratch");
+    cudaError_t e = launch_render_wavefront(d, cam, *p, accum, ctx->d_segments, next_counter(ctx), ctx->d_err, scratch,
+                                            topts.sort != 0, st);
+    cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "render launch");
+    return RT_SUCCESS;
+  }
+  cudaError_t e = launch_render(d, cam, *p, accum, ctx->d_segments, ctx->d_err, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render launch");
   return RT_SUCCESS;
 }
@@ -667,6 +688,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.sort = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "render.mode") {
+    if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
+    ctx->render_opts.mode = (int)value;
+    return RT_SUCCESS;
+  }
   ctx->last_error = "rtSetTuning: unknown key " + k;
   return RT_ERR_INVALID_ARGUMENT;
 }
@@ -681,6 +707,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.sort") {
     *value = ctx->trace_opts.sort;
+    return RT_SUCCESS;
+  }
+  if (k == "render.mode") {
+    *value = ctx->render_opts.mode;
     return RT_SUCCESS;
   }
   return RT_ERR_INVALID_ARGUMENT;

@@ -9,6 +9,8 @@
 // counting sort over the 2^20 buckets produces a permutation; the caster
 // then reads rays through it and writes each hit back to its input slot.
 // Order inside a bucket is arbitrary; results do not depend on the order.
+// With a device-side count (d_n), only the first *d_n rays of the buffer
+// take part (the launch is sized for the buffer's capacity n).
 #include <cuda_runtime.h>
 
 #include "rt_internal.h"
@@ -51,7 +53,8 @@ __device__ __forceinline__ void ray_coords(const float4 *rays, uint32_t i, float
 }
 
 // ext[0..4] = ordered min, ext[5..9] = ordered max (initialised by the host).
-__global__ void k_extent(const float4 *__restrict__ rays, uint32_t n, uint32_t *ext) {
+__global__ void k_extent(const float4 *__restrict__ rays, uint32_t n, const uint32_t *d_n, uint32_t *ext) {
+  if (d_n) n = min(n, *d_n);
   float lo[5], hi[5];
   for (int k = 0; k < 5; k++) {
     lo[k] = __int_as_float(0x7f800000);
@@ -108,8 +111,9 @@ __device__ __forceinline__ uint32_t ray_key(const float4 *rays, uint32_t i, cons
   return key;
 }
 
-__global__ void k_hist(const float4 *__restrict__ rays, uint32_t n, const uint32_t *ext, uint32_t *keys,
-                       uint32_t *hist) {
+__global__ void k_hist(const float4 *__restrict__ rays, uint32_t n, const uint32_t *d_n, const uint32_t *ext,
+                       uint32_t *keys, uint32_t *hist) {
+  if (d_n) n = min(n, *d_n);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t k = ray_key(rays, i, ext);
@@ -117,7 +121,9 @@ __global__ void k_hist(const float4 *__restrict__ rays, uint32_t n, const uint32
   atomicAdd(hist + k, 1u);
 }
 
-__global__ void k_scatter(const uint32_t *__restrict__ keys, uint32_t n, uint32_t *offsets, uint32_t *perm) {
+__global__ void k_scatter(const uint32_t *__restrict__ keys, uint32_t n, const uint32_t *d_n, uint32_t *offsets,
+                          uint32_t *perm) {
+  if (d_n) n = min(n, *d_n);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t slot = atomicAdd(offsets + keys[i], 1u);
@@ -139,7 +145,8 @@ size_t raysort_scratch_bytes(uint32_t n) {
   return 4ull * (16 + n + kBuckets + (kBuckets / 1024 + 2) + n);
 }
 
-cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, void *scratch, uint32_t **perm_out, cudaStream_t st) {
+cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, const uint32_t *d_n, void *scratch, uint32_t **perm_out,
+                           cudaStream_t st) {
   uint32_t *ext = static_cast<uint32_t *>(scratch);
   uint32_t *keys = ext + 16;
   uint32_t *hist = keys + n;
@@ -148,13 +155,13 @@ cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, void *scratch, uint32
   *perm_out = perm;
   const float4 *r = reinterpret_cast<const float4 *>(rays);
   k_init_ext<<<1, 32, 0, st>>>(ext);
-  k_extent<<<304, 256, 0, st>>>(r, n, ext);
+  k_extent<<<304, 256, 0, st>>>(r, n, d_n, ext);
   cudaError_t e = cudaMemsetAsync(hist, 0, 4ull * kBuckets, st);
   if (e != cudaSuccess) return e;
-  k_hist<<<(n + 255) / 256, 256, 0, st>>>(r, n, ext, keys, hist);
+  k_hist<<<(n + 255) / 256, 256, 0, st>>>(r, n, d_n, ext, keys, hist);
   e = exclusive_scan_u32(hist, hist, sums, kBuckets, st);
   if (e != cudaSuccess) return e;
-  k_scatter<<<(n + 255) / 256, 256, 0, st>>>(keys, n, hist, perm);
+  k_scatter<<<(n + 255) / 256, 256, 0, st>>>(keys, n, d_n, hist, perm);
   return cudaGetLastError();
 }
 

@@ -72,7 +72,9 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
 // Morton bucketing of a ray batch (raysort.cu); `scratch` holds
 // raysort_scratch_bytes(n); *perm_out points into it.
 size_t raysort_scratch_bytes(uint32_t n);
-cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, void *scratch, uint32_t **perm_out, cudaStream_t st);
+// With d_n != NULL only the first *d_n of the n rays are sorted.
+cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, const uint32_t *d_n, void *scratch, uint32_t **perm_out,
+                           cudaStream_t st);
 // The shader-literal 16-entry-stack traversal over the Bvh.h node array.
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
                                    cudaStream_t st);
@@ -81,6 +83,19 @@ cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint3
 // `segments` (may be NULL) accumulates the number of traced ray segments.
 cudaError_t launch_render(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
                           unsigned long long *segments, uint32_t *err, cudaStream_t st);
+
+// Wavefront render (wavefront.cu): same images as launch_render; `scratch`
+// holds wavefront_scratch_bytes(width*height); `counter` is a launch-private
+// device word.
+size_t wavefront_scratch_bytes(uint32_t cap);
+cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
+                                    unsigned long long *segments, uint32_t *counter, uint32_t *err, void *scratch,
+                                    bool sort, cudaStream_t st);
+
+// Render launch-shape knobs (rtSetTuning "render.mode").
+struct RenderOpts {
+  int mode = 2;  // 0 megakernel, 1 wavefront, 2 choose by image size
+};
 
 struct BatchJob {
   DevScene sc;

@@ -119,31 +119,10 @@ __device__ __forceinline__ PathState path_state(const DevScene &sc, uint32_t fla
   return ps;
 }
 
-// Closest hit of a path segment: triangles through the BVH, then spheres.
-template <int STACK>
-__device__ __forceinline__ bool closest_hit(const DevScene &sc, const PathState &ps, f3 o, f3 d, HitRec &rec,
-                                            uint32_t *err) {
-  float closest = kTmax, u = 0.0f, v = 0.0f;
-  bool hit = false;
-  if (ps.flags & RT_COMPAT_STACK16) {
-    int ti = traverse_literal16(sc, o, d, kTmin, closest, u, v);
-    if (ti >= 0) {
-      const rt_triangle tr = sc.tris[ti];
-      f3 v0 = ld3(tr.v0), v1 = ld3(tr.v1), v2 = ld3(tr.v2);
-      triangle_record(o, d, closest, cross3(sub3(v2, v0), sub3(v0, v1)), tr.material_index, rec);
-      hit = true;
-    }
-  } else {
-    TraceRay r = make_ray(o, d, kTmin);
-    int k = traverse_closest<STACK>(sc, r, closest, u, v, err);
-    if (k >= 0) {
-      const float4 *T = sc.tpre + 3ll * k;
-      float4 t0 = __ldg(T), t1 = __ldg(T + 1);
-      uint32_t mat = __ldg(&sc.tris[__ldg(sc.leaf_tri + k)].material_index);
-      triangle_record(o, d, closest, mk3(t0.w, t1.x, t1.y), mat, rec);
-      hit = true;
-    }
-  }
+// Spheres after the BVH: with `closest` carried over (true closest hit),
+// reset to tmax as the reference's hit_scene does (comp:236), or skipped.
+__device__ __forceinline__ bool sphere_pass(const DevScene &sc, const PathState &ps, f3 o, f3 d, bool hit,
+                                            HitRec &rec) {
   if (ps.sphere_mode != 0) {
     float lim = (ps.sphere_mode == 2) ? kTmax : (hit ? rec.t : kTmax);
     for (uint32_t j = 0; j < ps.nspheres; j++) {
@@ -156,6 +135,42 @@ __device__ __forceinline__ bool closest_hit(const DevScene &sc, const PathState 
     }
   }
   return hit;
+}
+
+// Record of the triangle leaf k (position in tpre) hit at t, then the sphere
+// pass. Shared by the megakernel and the wavefront shade step.
+__device__ __forceinline__ bool resolve_hit(const DevScene &sc, const PathState &ps, f3 o, f3 d, int k,
+                                            float closest, HitRec &rec) {
+  bool hit = false;
+  if (k >= 0) {
+    const float4 *T = sc.tpre + 3ll * k;
+    float4 t0 = __ldg(T), t1 = __ldg(T + 1);
+    uint32_t mat = __ldg(&sc.tris[__ldg(sc.leaf_tri + k)].material_index);
+    triangle_record(o, d, closest, mk3(t0.w, t1.x, t1.y), mat, rec);
+    hit = true;
+  }
+  return sphere_pass(sc, ps, o, d, hit, rec);
+}
+
+// Closest hit of a path segment: triangles through the BVH, then spheres.
+template <int STACK>
+__device__ __forceinline__ bool closest_hit(const DevScene &sc, const PathState &ps, f3 o, f3 d, HitRec &rec,
+                                            uint32_t *err) {
+  float closest = kTmax, u = 0.0f, v = 0.0f;
+  if (ps.flags & RT_COMPAT_STACK16) {
+    bool hit = false;
+    int ti = traverse_literal16(sc, o, d, kTmin, closest, u, v);
+    if (ti >= 0) {
+      const rt_triangle tr = sc.tris[ti];
+      f3 v0 = ld3(tr.v0), v1 = ld3(tr.v1), v2 = ld3(tr.v2);
+      triangle_record(o, d, closest, cross3(sub3(v2, v0), sub3(v0, v1)), tr.material_index, rec);
+      hit = true;
+    }
+    return sphere_pass(sc, ps, o, d, hit, rec);
+  }
+  TraceRay r = make_ray(o, d, kTmin);
+  int k = traverse_closest<STACK>(sc, r, closest, u, v, err);
+  return resolve_hit(sc, ps, o, d, k, closest, rec);
 }
 
 // random_in_unit_sphere (random.glsl:29-32) through random(min, max) (24-27).
