@@ -198,9 +198,27 @@ typedef struct rt_render_job {
   float *d_rgba32f;
 } rt_render_job;
 
-/* Renders every job with one persistent launch; per job the result equals
- * rtRender of that job alone. */
+/* Renders every job with one persistent launch over the pixel tiles of all
+ * jobs; per job the image equals rtRender of that job alone (megakernel
+ * arithmetic). The reference renders one scene per dispatch
+ * (src/main.cpp:228); this is the batched form. Stream-ordered; the job
+ * table is copied to the device inside the call. */
 rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, void *stream);
+
+/* A resident job table for repeated batched launches. Scenes named by the
+ * jobs must stay resident while the batch exists. */
+typedef struct rt_batch rt_batch;
+rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, rt_batch **out);
+rt_status rtBatchDestroy(rt_ctx *ctx, rt_batch *batch);
+/* One persistent launch over the batch; performs no host synchronisation
+ * and no allocation, so it can be captured in a CUDA graph. */
+rt_status rtBatchLaunch(rt_ctx *ctx, rt_batch *batch, void *stream);
+/* Adds each job's spp to its sample_index on the device (the next
+ * progressive frame); capturable. */
+rt_status rtBatchAdvance(rt_ctx *ctx, rt_batch *batch, void *stream);
+/* rtBatchLaunch followed by rtBatchAdvance, replayed from a CUDA graph that
+ * the first call captures and instantiates (one graph launch per frame). */
+rt_status rtBatchLaunchGraph(rt_ctx *ctx, rt_batch *batch, void *stream);
 
 #ifdef __cplusplus
 }

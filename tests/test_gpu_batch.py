@@ -1,0 +1,96 @@
+"""Batched rendering: many scenes of uneven size in one persistent launch.
+Each job's image must equal the job rendered alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def scenes(rt, ctx, specs):
+    out = []
+    for seed, n_soup, n_sph in specs:
+        t, m, s = rt.gen_cornell(seed, n_soup, n_sph, 0.2, 1.0)
+        out.append(ctx.upload_scene(t, m, spheres=s))
+    return out
+
+
+SPECS = [(31, 200, 0), (32, 3000, 4), (33, 20000, 16), (34, 1000, 2), (35, 60000, 8)]
+SIZES = [(64, 48), (128, 128), (96, 80), (40, 200), (160, 96)]
+
+
+def render_alone(ctx, sc, cam, W, H, spp, bounces, flags=0, sample_index=0):
+    import torch
+    acc = torch.zeros((H, W, 4), device="cuda")
+    sc.set_camera(cam)
+    sc.render(acc, W, H, spp=spp, max_bounces=bounces, flags=flags, sample_index=sample_index)
+    ctx.synchronize()
+    return acc.cpu().numpy()
+
+
+def test_batch_equals_individual_renders(rt, ctx):
+    import torch
+    scs = scenes(rt, ctx, SPECS)
+    try:
+        jobs, accs, want = [], [], []
+        for i, (sc, (W, H)) in enumerate(zip(scs, SIZES)):
+            cam = rt.camera_look_at([0.3 * i, 0.2, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
+            spp, bounces = 1 + i % 3, 3 + i
+            flags = rt.COMPAT_LEN1 if i == 3 else 0
+            acc = torch.zeros((H, W, 4), device="cuda")
+            accs.append(acc)
+            jobs.append(rt.make_job(sc, cam, acc, W, H, spp, bounces, 0, flags))
+            want.append(render_alone(ctx, sc, cam, W, H, spp, bounces, flags))
+        ctx.segments(reset=True)
+        ctx.render_batch(jobs)
+        ctx.synchronize()
+        assert ctx.segments(reset=True) > 0
+        for a, w in zip(accs, want):
+            assert np.array_equal(a.cpu().numpy().view(np.uint32), w.view(np.uint32))
+    finally:
+        for sc in scs:
+            sc.release()
+
+
+def test_batch_graph_progressive_frames(rt, ctx):
+    """Three graph replays (launch + device-side sample advance) equal one
+    render of three times the samples."""
+    import torch
+    scs = scenes(rt, ctx, SPECS[:3])
+    try:
+        jobs, accs, want = [], [], []
+        for i, (sc, (W, H)) in enumerate(zip(scs, SIZES)):
+            cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
+            acc = torch.zeros((H, W, 4), device="cuda")
+            accs.append(acc)
+            jobs.append(rt.make_job(sc, cam, acc, W, H, 2, 6))
+            want.append(render_alone(ctx, sc, cam, W, H, 6, 6))
+        b = ctx.batch(jobs)
+        try:
+            for _ in range(3):
+                b.launch_graph()
+            ctx.synchronize()
+        finally:
+            b.destroy()
+        for a, w in zip(accs, want):
+            assert np.array_equal(a.cpu().numpy().view(np.uint32), w.view(np.uint32))
+    finally:
+        for sc in scs:
+            sc.release()
+
+
+def test_batch_rejects_bad_jobs(rt, ctx):
+    import torch
+    t, m, s = rt.gen_cornell(1, 10)
+    sc = ctx.upload_scene(t, m)
+    try:
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 8, 8)
+        acc = torch.zeros((8, 8, 4), device="cuda")
+        good = rt.make_job(sc, cam, acc, 8, 8)
+        bad = rt.RenderJob(9999, 0, cam, rt.RenderParams(8, 8, 1, 8, 0, 0), acc.data_ptr())
+        with pytest.raises(rt.RtError):
+            ctx.render_batch([good, bad])
+        zero = rt.make_job(sc, cam, acc, 0, 8)
+        with pytest.raises(rt.RtError):
+            ctx.render_batch([zero])
+    finally:
+        sc.release()

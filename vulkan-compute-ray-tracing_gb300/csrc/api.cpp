@@ -730,14 +730,156 @@ rt_status rtSynchronize(rt_ctx *ctx, void *stream) {
   return RT_SUCCESS;
 }
 
+}  // extern "C"
+
+struct rt_batch {
+  BatchJob *d_jobs = nullptr;
+  uint32_t n = 0, total_tiles = 0, max_depth = 0;
+  uint32_t *counter = nullptr;
+  cudaStream_t capture = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Validates the jobs and lays out their tiles; fills host BatchJob records.
+rt_status make_jobs(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n, std::vector<BatchJob> &out,
+                    uint32_t &total_tiles, uint32_t &max_depth) {
+  out.resize(n);
+  uint64_t tiles = 0;
+  max_depth = 1;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  for (uint32_t j = 0; j < n; j++) {
+    const rt_render_job &J = jobs[j];
+    Scene *sc = find_scene(ctx, J.scene);
+    if (!sc) {
+      ctx->last_error = "batch job " + std::to_string(j) + ": scene not found";
+      return RT_ERR_NOT_FOUND;
+    }
+    const rt_render_params &p = J.params;
+    if (!J.d_rgba32f || (uintptr_t)J.d_rgba32f % 16 || p.width == 0 || p.height == 0 || p.width > 65536 ||
+        p.height > 65536) {
+      ctx->last_error = "batch job " + std::to_string(j) + ": bad image or size";
+      return RT_ERR_INVALID_ARGUMENT;
+    }
+    BatchJob &B = out[j];
+    B.sc = sc->dev;
+    B.cam = J.camera;
+    B.p = p;
+    B.accum = J.d_rgba32f;
+    B.tile_begin = (uint32_t)tiles;
+    B.tiles_x = batch_tiles_x(p.width);
+    tiles += batch_tiles(p.width, p.height);
+    max_depth = std::max(max_depth, sc->dev.depth);
+  }
+  if (tiles >= (1ull << 32)) {
+    ctx->last_error = "batch has too many tiles";
+    return RT_ERR_INVALID_ARGUMENT;
+  }
+  total_tiles = (uint32_t)tiles;
+  return RT_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, rt_batch **out) {
+  if (!ctx || !out || (n_jobs && !jobs)) return RT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::vector<BatchJob> host;
+  uint32_t total = 0, depth = 1;
+  rt_status s = make_jobs(ctx, jobs, n_jobs, host, total, depth);
+  if (s != RT_SUCCESS) return s;
+  rt_batch *b = new rt_batch();
+  b->n = n_jobs;
+  b->total_tiles = total;
+  b->max_depth = depth;
+  cudaError_t e = cudaMalloc((void **)&b->d_jobs, sizeof(BatchJob) * std::max(n_jobs, 1u));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->counter, 256);
+  if (e == cudaSuccess && n_jobs)
+    e = cudaMemcpy(b->d_jobs, host.data(), sizeof(BatchJob) * n_jobs, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    rtBatchDestroy(ctx, b);
+    return cuda_fail(ctx, e, "batch creation");
+  }
+  *out = b;
+  return RT_SUCCESS;
+}
+
+rt_status rtBatchDestroy(rt_ctx *ctx, rt_batch *b) {
+  if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->capture) cudaStreamDestroy(b->capture);
+  if (b->d_jobs) cudaFree(b->d_jobs);
+  if (b->counter) cudaFree(b->counter);
+  delete b;
+  return RT_SUCCESS;
+}
+
+rt_status rtBatchLaunch(rt_ctx *ctx, rt_batch *b, void *stream) {
+  if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
+  CK(launch_render_batch(b->d_jobs, b->n, b->total_tiles, b->max_depth, b->counter, ctx->d_segments, ctx->d_err,
+                         pick_stream(ctx, stream)),
+     "batch launch");
+  return RT_SUCCESS;
+}
+
+rt_status rtBatchAdvance(rt_ctx *ctx, rt_batch *b, void *stream) {
+  if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
+  CK(launch_batch_advance(b->d_jobs, b->n, pick_stream(ctx, stream)), "batch advance");
+  return RT_SUCCESS;
+}
+
+rt_status rtBatchLaunchGraph(rt_ctx *ctx, rt_batch *b, void *stream) {
+  if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
+  if (!b->exec) {
+    CK(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "graph capture");
+    cudaError_t e = launch_render_batch(b->d_jobs, b->n, b->total_tiles, b->max_depth, b->counter, ctx->d_segments,
+                                        ctx->d_err, b->capture);
+    if (e == cudaSuccess) e = launch_batch_advance(b->d_jobs, b->n, b->capture);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(b->capture, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return cuda_fail(ctx, e != cudaSuccess ? e : e2, "graph capture");
+    }
+    b->graph = g;
+    CK(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+  }
+  CK(cudaGraphLaunch(b->exec, pick_stream(ctx, stream)), "graph launch");
+  return RT_SUCCESS;
+}
+
 rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, void *stream) {
   if (!ctx || (n_jobs && !jobs)) return RT_ERR_INVALID_ARGUMENT;
-  for (uint32_t j = 0; j < n_jobs; j++) {
-    rt_status s = rtSetCamera(ctx, jobs[j].scene, &jobs[j].camera);
-    if (s != RT_SUCCESS) return s;
-    s = rtRender(ctx, jobs[j].scene, &jobs[j].params, jobs[j].d_rgba32f, stream);
-    if (s != RT_SUCCESS) return s;
-  }
+  if (n_jobs == 0) return RT_SUCCESS;
+  std::vector<BatchJob> host;
+  uint32_t total = 0, depth = 1;
+  rt_status s = make_jobs(ctx, jobs, n_jobs, host, total, depth);
+  if (s != RT_SUCCESS) return s;
+  cudaStream_t st = pick_stream(ctx, stream);
+  // Job table and tile counter from the stream-ordered pool; the table is
+  // staged through pinned memory so the copy is asynchronous.
+  BatchJob *d_jobs = nullptr;
+  uint32_t *counter = nullptr;
+  CK(cudaMallocAsync((void **)&d_jobs, sizeof(BatchJob) * n_jobs + 256, st), "batch table");
+  counter = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(d_jobs) + sizeof(BatchJob) * n_jobs);
+  BatchJob *pinned = nullptr;
+  CK(cudaMallocHost((void **)&pinned, sizeof(BatchJob) * n_jobs), "batch staging");
+  std::memcpy(pinned, host.data(), sizeof(BatchJob) * n_jobs);
+  cudaError_t e = cudaMemcpyAsync(d_jobs, pinned, sizeof(BatchJob) * n_jobs, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = launch_render_batch(d_jobs, n_jobs, total, depth, counter, ctx->d_segments, ctx->d_err, st);
+  cudaFreeAsync(d_jobs, st);
+  // The staging buffer must outlive the copy.
+  cudaStreamSynchronize(st);
+  cudaFreeHost(pinned);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batch launch");
   return RT_SUCCESS;
 }
 

@@ -97,17 +97,22 @@ struct RenderOpts {
   int mode = 2;  // 0 megakernel, 1 wavefront, 2 choose by image size
 };
 
+// One job of a batched render (render.cu: k_render_batch).
 struct BatchJob {
   DevScene sc;
   rt_camera cam;
   rt_render_params p;
   float *accum;
   uint32_t tile_begin;  // first tile of this job in the batch's tile space
-  uint32_t tiles_x;     // tiles per row
+  uint32_t tiles_x;     // tiles per image row
 };
-cudaError_t launch_render_batch(const BatchJob *d_jobs, uint32_t n_jobs, uint32_t total_tiles,
-                                const uint32_t *d_tile_job, uint32_t *d_counter, uint32_t *err,
-                                cudaStream_t st);
+uint32_t batch_tiles_x(uint32_t width);
+uint32_t batch_tiles(uint32_t width, uint32_t height);
+// d_jobs sorted by tile_begin; max_depth = deepest BVH among the jobs.
+cudaError_t launch_render_batch(const BatchJob *d_jobs, uint32_t n_jobs, uint32_t total_tiles, uint32_t max_depth,
+                                uint32_t *counter, unsigned long long *segments, uint32_t *err, cudaStream_t st);
+// sample_index += spp for every job (the next progressive frame).
+cudaError_t launch_batch_advance(BatchJob *d_jobs, uint32_t n_jobs, cudaStream_t st);
 
 // ---------------------------------------------------------------- bvh_build.cu
 // Builds the Bvh.h node array on the GPU. `axes` holds rand() % 3 for every

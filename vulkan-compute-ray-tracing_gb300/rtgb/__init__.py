@@ -114,6 +114,12 @@ def _load() -> ctypes.CDLL:
         "rtGetTuning": (I32, [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),
         "rtReadSegmentCounter": (I32, [P, ctypes.POINTER(U64), I32]),
         "rtRenderBatch": (I32, [P, ctypes.POINTER(RenderJob), U32, P]),
+        "rtBatchCreate": (I32, [P, ctypes.POINTER(RenderJob), U32, ctypes.POINTER(P)]),
+        "rtBatchDestroy": (I32, [P, P]),
+        "rtBatchLaunch": (I32, [P, P, P]),
+        "rtBatchAdvance": (I32, [P, P, P]),
+        "rtBatchLaunchGraph": (I32, [P, P, P]),
+        "rtBuildBvhNoAlloc": (I32, [P, U32, U32, P, P]),
         "rtgbGenCornell": (U32, [U64, U32, U32, F32, F32, F32, P, P, P]),
         "rtgbGenIcosphere": (U32, [U64, U32, F32, F32, U32, P]),
         "rtgbGenCameraRays": (None, [ctypes.POINTER(Camera), U32, U32, F32, F32, P]),
@@ -292,6 +298,40 @@ class Context:
     def render_batch(self, jobs, stream=None):
         arr = (RenderJob * len(jobs))(*jobs)
         self.check(LIB.rtRenderBatch(self.handle, arr, len(jobs), stream), "rtRenderBatch")
+
+    def batch(self, jobs) -> "Batch":
+        arr = (RenderJob * len(jobs))(*jobs)
+        h = ctypes.c_void_p()
+        self.check(LIB.rtBatchCreate(self.handle, arr, len(jobs), ctypes.byref(h)), "rtBatchCreate")
+        return Batch(self, h)
+
+
+def make_job(scene: "Scene", cam: Camera, accum, width: int, height: int, spp: int = 1, max_bounces: int = 8,
+             sample_index: int = 0, flags: int = 0) -> RenderJob:
+    return RenderJob(scene.id, 0, cam, RenderParams(width, height, spp, max_bounces, sample_index, flags),
+                     _ptr(accum))
+
+
+class Batch:
+    """A resident job table (rtBatchCreate) launched as one persistent kernel."""
+
+    def __init__(self, ctx: "Context", handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def launch(self, stream=None):
+        self.ctx.check(LIB.rtBatchLaunch(self.ctx.handle, self.handle, stream), "rtBatchLaunch")
+
+    def advance(self, stream=None):
+        self.ctx.check(LIB.rtBatchAdvance(self.ctx.handle, self.handle, stream), "rtBatchAdvance")
+
+    def launch_graph(self, stream=None):
+        self.ctx.check(LIB.rtBatchLaunchGraph(self.ctx.handle, self.handle, stream), "rtBatchLaunchGraph")
+
+    def destroy(self):
+        if self.handle:
+            self.ctx.check(LIB.rtBatchDestroy(self.ctx.handle, self.handle), "rtBatchDestroy")
+            self.handle = None
 
 
 class Scene:
