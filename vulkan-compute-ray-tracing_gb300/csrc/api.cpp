@@ -135,6 +135,25 @@ uint32_t check_tree(const rt_bvh_node *nodes, uint32_t nn, uint32_t ntris, std::
   return depth;
 }
 
+struct SlabLayout {
+  size_t tris, mats, lights, spheres, nodes, bvh2, tpre, leaf, total;
+};
+
+SlabLayout slab_layout(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
+  const uint32_t nnodes = 2 * nt - 1, ninner = nt > 1 ? nt - 1 : 1;
+  SlabLayout L;
+  L.tris = 0;
+  L.mats = L.tris + align256(sizeof(rt_triangle) * nt);
+  L.lights = L.mats + align256(sizeof(rt_material) * nm);
+  L.spheres = L.lights + align256(sizeof(rt_light) * std::max(nl, 1u));
+  L.nodes = L.spheres + align256(sizeof(rt_sphere) * std::max(ns, 1u));
+  L.bvh2 = L.nodes + align256(sizeof(rt_bvh_node) * nnodes);
+  L.tpre = L.bvh2 + align256(64ull * ninner);
+  L.leaf = L.tpre + align256(48ull * nt);
+  L.total = L.leaf + align256(4ull * nt);
+  return L;
+}
+
 Scene *find_scene(rt_ctx *ctx, rt_scene_id id) {
   auto it = ctx->scenes.find(id);
   if (it == ctx->scenes.end()) return nullptr;
@@ -336,16 +355,9 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   }
 
   // One slab per scene.
-  const uint32_t ninner = nt > 1 ? nt - 1 : 1;
-  size_t off_tris = 0;
-  size_t off_mats = off_tris + align256(sizeof(rt_triangle) * nt);
-  size_t off_lights = off_mats + align256(sizeof(rt_material) * nm);
-  size_t off_spheres = off_lights + align256(sizeof(rt_light) * std::max(nl, 1u));
-  size_t off_nodes = off_spheres + align256(sizeof(rt_sphere) * std::max(ns, 1u));
-  size_t off_bvh2 = off_nodes + align256(sizeof(rt_bvh_node) * nnodes);
-  size_t off_tpre = off_bvh2 + align256(64ull * ninner);
-  size_t off_leaf = off_tpre + align256(48ull * nt);
-  size_t total = off_leaf + align256(4ull * nt);
+  SlabLayout L = slab_layout(nt, nm, nl, ns);
+  size_t off_tris = L.tris, off_mats = L.mats, off_lights = L.lights, off_spheres = L.spheres, off_nodes = L.nodes,
+         off_bvh2 = L.bvh2, off_tpre = L.tpre, off_leaf = L.leaf, total = L.total;
   {
     std::lock_guard<std::mutex> g(ctx->mu);
     if (ctx->used + total > ctx->budget)
@@ -731,6 +743,25 @@ rt_status rtSynchronize(rt_ctx *ctx, void *stream) {
 }
 
 }  // extern "C"
+
+namespace rtgb {
+
+bool ctx_scene_dev(rt_ctx *ctx, rt_scene_id id, DevScene *out) {
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Scene *sc = find_scene(ctx, id);
+  if (!sc) return false;
+  *out = sc->dev;
+  return true;
+}
+unsigned long long *ctx_segments(rt_ctx *ctx) { return ctx->d_segments; }
+uint32_t *ctx_err(rt_ctx *ctx) { return ctx->d_err; }
+uint64_t ctx_budget(rt_ctx *ctx) { return ctx->budget; }
+int ctx_device(rt_ctx *ctx) { return ctx->device; }
+uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
+  return nt ? slab_layout(nt, nm, nl, ns).total : 0;
+}
+
+}  // namespace rtgb
 
 struct rt_batch {
   BatchJob *d_jobs = nullptr;

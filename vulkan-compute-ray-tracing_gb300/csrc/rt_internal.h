@@ -120,6 +120,16 @@ cudaError_t launch_batch_advance(BatchJob *d_jobs, uint32_t n_jobs, cudaStream_t
 rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_axes, rt_bvh_node *d_nodes,
                         cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen);
 
+// ---------------------------------------------------------------- api.cpp
+// Context internals for the serving layer (serve.cpp).
+bool ctx_scene_dev(rt_ctx *ctx, rt_scene_id id, DevScene *out);
+unsigned long long *ctx_segments(rt_ctx *ctx);
+uint32_t *ctx_err(rt_ctx *ctx);
+uint64_t ctx_budget(rt_ctx *ctx);
+int ctx_device(rt_ctx *ctx);
+// Device bytes rtUploadScene allocates for a scene of these counts.
+uint64_t scene_device_bytes(uint32_t n_triangles, uint32_t n_materials, uint32_t n_lights, uint32_t n_spheres);
+
 // ---------------------------------------------------------------- glibc_rand.cpp
 // glibc's TYPE_3 random() (what rand() returns) after srand(seed).
 void glibc_rand_axes(uint32_t seed, uint64_t count, uint8_t *out_mod3);
