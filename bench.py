@@ -33,7 +33,6 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -134,30 +133,18 @@ def make_workload(rt):
 
 
 def dist_init():
-    import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    return world, rank, local
+    from rtgb import replicas
+    return replicas.init()
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from rtgb import replicas
+    replicas.barrier(world)
 
 
 def max_over_ranks(x: float, world: int) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from rtgb import replicas
+    return replicas.max_over_ranks(x, world)
 
 
 def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 30.0):
@@ -327,6 +314,172 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
+def _line(workload, metric, value, unit, args, extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+         "data": "synthetic (seeded)", "config": {"workload": workload}}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def run_render(args):
+    """Config 0: Cornell box + 12,000 soup triangles, 256x256, 1 spp, 8 bounces."""
+    import torch
+    import rtgb
+    ctx = rtgb.Context(0)
+    t, m, s = rtgb.gen_cornell(1, 12000, 0)
+    sc = ctx.upload_scene(t, m)
+    W = H = 256
+    sc.set_camera(rtgb.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    acc = torch.zeros((H, W, 4), device="cuda")
+    host = torch.empty((H, W, 4)).pin_memory()
+    for k in range(args.warmup):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    ctx.segments(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=args.warmup + k, stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    seg = ctx.segments(reset=True)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=stream.cuda_stream)
+        host.copy_(acc, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    seg2 = ctx.segments(reset=True)
+    _line("render 256x256 1spp 8 bounces, Cornell box + 12,000 soup triangles", METRIC, seg / (ms / 1e3) / 1e6,
+          "Mrays/s", args, {"ms_per_step": ms / args.steps, "segments_per_step": seg / args.steps,
+                            "e2e": {"value": seg2 / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                                    "d2h_bytes_per_step": W * H * 16}})
+    ctx.close()
+
+
+def run_batch(args):
+    """Config 2: many scenes of uneven size, batched launch vs one launch per render."""
+    import torch
+    import rtgb
+    from rtgb import workloads as wl
+    ctx = rtgb.Context(0)
+    specs = wl.batch_scene_specs(args.batch_scenes)
+    scenes, jobs, accs = [], [], []
+    t0 = time.perf_counter()
+    build_ms = 0.0
+    tris_total = 0
+    for sp in specs:
+        t, m, s = wl.make_scene(sp)
+        sc = ctx.upload_scene(t, m, spheres=s)
+        build_ms += sc.info().build_ms
+        tris_total += len(t)
+        scenes.append(sc)
+        acc = torch.zeros((sp.side, sp.side, 4), device="cuda")
+        accs.append(acc)
+        jobs.append(rtgb.make_job(sc, wl.default_camera(sp.side), acc, sp.side, sp.side, 4, 8))
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+
+    def plain():
+        for sc, sp, acc in zip(scenes, specs, accs):
+            sc.set_camera(wl.default_camera(sp.side))
+            sc.render(acc, sp.side, sp.side, spp=4, max_bounces=8, stream=sptr)
+
+    b = ctx.batch(jobs)
+    res = {}
+    for name, fn in (("plain", plain), ("batched", lambda: b.launch(sptr)), ("batched_graph", lambda: b.launch_graph(sptr))):
+        fn()  # warm-up
+        torch.cuda.synchronize()
+        ctx.segments(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        seg = ctx.segments(reset=True) / args.steps
+        res[name] = {"ms_per_batch": ms, "mrays_s": seg / (ms / 1e3) / 1e6, "renders_s": len(jobs) / (ms / 1e3)}
+    b.destroy()
+    _line(f"batched render: {len(jobs)} scenes ({tris_total} triangles), sides 128-1024, 4 spp, 8 bounces",
+          METRIC, res["batched_graph"]["mrays_s"], "Mrays/s", args,
+          {"modes": res, "speedup_vs_plain": res["batched_graph"]["renders_s"] / res["plain"]["renders_s"],
+           "setup_s": setup_s, "bvh_build_ms_total": build_ms})
+    ctx.close()
+
+
+def run_serve(args):
+    """Config 3: open-loop Poisson requests over resident scenes; continuous
+    batching vs one request per launch."""
+    import rtgb
+    from rtgb import serve
+    from rtgb import workloads as wl
+    ctx = rtgb.Context(0)
+    specs = wl.batch_scene_specs(args.serve_scenes, base_seed=2000)
+    datas = [wl.make_scene(sp) for sp in specs]
+    sides = tuple(int(x) for x in args.serve_sides.split(","))
+    out = {}
+    for rate in [float(x) for x in args.serve_rates.split(",")]:
+        reqs = wl.request_stream(args.serve_requests, rate, len(specs), sides=sides, spp_max=args.serve_spp_max)
+        for mode, kw in (("continuous", dict(max_active=args.serve_active, spp_per_step=args.serve_step)),
+                         ("plain", dict(max_active=1, spp_per_step=0))):
+            with serve.Server(ctx, hbm_budget_bytes=150 << 30, **kw) as srv:
+                handles = [srv.add_scene(*d) for d in datas]
+                warm = [srv.submit(h, wl.default_camera(8), 8, 8, 1, 1, keep_image=False) for h in handles]
+                for w in warm:
+                    srv.wait(w)
+                srv.reset_stats()
+                wall, ids = wl.run_stream(srv, handles, reqs)
+                st = srv.stats()
+                out[f"{mode}@{rate:g}"] = {"renders_s": len(reqs) / wall, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
+                                           "mean_ms": st.mean_ms, "steps": st.steps, "wall_s": wall,
+                                           "uploads": st.scene_uploads, "evictions": st.scene_evictions}
+    best = max(v["renders_s"] for k, v in out.items() if k.startswith("continuous"))
+    _line(f"served renders: {args.serve_requests} Poisson requests per rate over {len(specs)} resident scenes, "
+          f"sides {sides}, spp 1-{args.serve_spp_max}, 8 bounces", METRIC, best, "renders/s", args,
+          {"rates": out})
+    ctx.close()
+
+
+def run_large(args):
+    """Config 4: ~8M triangles (6x6 grid of flattened displaced level-7
+    icospheres + the Cornell box), 1920x1080, 1 spp per frame, 8 bounces."""
+    import torch
+    import rtgb
+    ctx = rtgb.Context(0)
+    t, m = rtgb.gen_grid(4, 6, 6, 7, 0.35, 0.05, 222222, 3.0)
+    sc = ctx.upload_scene(t, m)
+    info = sc.info()
+    W, H = 1920, 1080
+    sc.set_camera(rtgb.camera_look_at([0, 2, -40], [0, -6, 0], [0, 1, 0], 40.0, W, H))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    acc = torch.zeros((H, W, 4), device="cuda")
+    frames = args.steps
+    sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=0, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    ctx.segments(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(frames):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    seg = ctx.segments(reset=True)
+    _line(f"progressive render 1920x1080, {frames} frames x 1 spp, 8 bounces, {info.triangles} triangles",
+          METRIC, seg / (ms / 1e3) / 1e6, "Mrays/s", args,
+          {"ms_per_frame": ms / frames, "bvh_build_ms": info.build_ms, "bvh_depth": info.depth,
+           "triangles": info.triangles})
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,9 +487,26 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="closest-hit", choices=["closest-hit", "render", "batch", "serve", "large"])
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--serve-scenes", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--serve-rates", default="1,4")
+    ap.add_argument("--serve-sides", default="256,512,1024")
+    ap.add_argument("--serve-spp-max", type=int, default=64)
+    ap.add_argument("--serve-active", type=int, default=64)
+    ap.add_argument("--serve-step", type=int, default=4)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "render":
+        run_render(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
+    elif args.workload == "large":
+        run_large(args)
     else:
         run_gpu(args)
 

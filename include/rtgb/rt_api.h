@@ -125,6 +125,14 @@ rt_status rtSetCamera(rt_ctx *ctx, rt_scene_id scene, const rt_camera *camera);
 rt_status rtRender(rt_ctx *ctx, rt_scene_id scene, const rt_render_params *params, float *d_rgba32f,
                    void *stream);
 
+/* Display epilogue of the reference's post-process shader
+ * (resources/shaders/source/post-process-shader.frag:62-68): each pixel of
+ * the RGBA32F image becomes pow(rgb, 1/gamma) with alpha 1, rounded to
+ * 8 bits per channel (clamped to [0,1]), into a device RGBA8 buffer of
+ * width*height*4 bytes. The reference uses gamma 2.2. Stream-ordered. */
+rt_status rtExportImage(rt_ctx *ctx, const float *d_rgba32f, uint32_t width, uint32_t height, float gamma,
+                        uint8_t *d_rgba8, void *stream);
+
 /* Closest-hit casting for a device batch of rays (the hit_bvh loop of
  * ray-trace-compute.comp:262-311 as a stand-alone query). Stream-ordered. */
 rt_status rtTraceClosest(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,

@@ -165,3 +165,24 @@ def test_wavefront_config0_vs_oracle(rt, orc, ctx):
         assert (mae(img, want) <= TOL).all()
     finally:
         sc.release()
+
+
+def test_export_gamma_rgba8(rt, ctx, tmp_path):
+    """post-process-shader.frag:67-68: pow(rgb, 1/2.2), alpha 1, 8 bits."""
+    import torch
+    rng = np.random.default_rng(3)
+    img = rng.uniform(-0.2, 1.5, (37, 53, 4)).astype(np.float32)
+    img[0, 0, :3] = [0.0, np.nan, np.inf]
+    d_in = torch.from_numpy(img).cuda()
+    d_out = torch.zeros((37, 53, 4), dtype=torch.uint8, device="cuda")
+    rt.export_image(ctx, d_in, 53, 37, d_out, gamma=2.2)
+    ctx.synchronize()
+    got = d_out.cpu().numpy().astype(np.int32)
+    with np.errstate(invalid="ignore"):
+        x = np.where(img[..., :3] > 0, np.power(np.maximum(img[..., :3], 0).astype(np.float64), 1 / 2.2), 0.0)
+    x = np.nan_to_num(x, nan=0.0, posinf=1.0)
+    want = np.rint(np.clip(x, 0, 1) * 255).astype(np.int32)
+    assert np.abs(got[..., :3] - want).max() <= 1
+    assert (got[..., 3] == 255).all()
+    rt.write_ppm(str(tmp_path / "x.ppm"), d_out.cpu().numpy())
+    assert (tmp_path / "x.ppm").stat().st_size == 37 * 53 * 3 + len(b"P6\n53 37\n255\n")

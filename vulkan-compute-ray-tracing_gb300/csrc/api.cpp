@@ -728,6 +728,16 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   return RT_ERR_INVALID_ARGUMENT;
 }
 
+rt_status rtExportImage(rt_ctx *ctx, const float *d_rgba32f, uint32_t width, uint32_t height, float gamma,
+                        uint8_t *d_rgba8, void *stream) {
+  if (!ctx || !d_rgba32f || !d_rgba8 || !(gamma > 0.0f) || (uintptr_t)d_rgba32f % 16 || (uintptr_t)d_rgba8 % 4)
+    return RT_ERR_INVALID_ARGUMENT;
+  uint64_t n = (uint64_t)width * height;
+  if (n >= (1ull << 32)) return RT_ERR_INVALID_ARGUMENT;
+  CK(launch_export(d_rgba32f, (uint32_t)n, gamma, d_rgba8, pick_stream(ctx, stream)), "export");
+  return RT_SUCCESS;
+}
+
 rt_status rtSynchronize(rt_ctx *ctx, void *stream) {
   if (!ctx) return RT_ERR_INVALID_ARGUMENT;
   CK(cudaStreamSynchronize(pick_stream(ctx, stream)), "synchronize");

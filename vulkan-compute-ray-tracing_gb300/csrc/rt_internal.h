@@ -120,6 +120,9 @@ cudaError_t launch_batch_advance(BatchJob *d_jobs, uint32_t n_jobs, cudaStream_t
 rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_axes, rt_bvh_node *d_nodes,
                         cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen);
 
+// ---------------------------------------------------------------- export.cu
+cudaError_t launch_export(const float *in, uint32_t n, float gamma, uint8_t *out, cudaStream_t st);
+
 // ---------------------------------------------------------------- api.cpp
 // Context internals for the serving layer (serve.cpp).
 bool ctx_scene_dev(rt_ctx *ctx, rt_scene_id id, DevScene *out);

@@ -120,6 +120,7 @@ def _load() -> ctypes.CDLL:
         "rtBatchAdvance": (I32, [P, P, P]),
         "rtBatchLaunchGraph": (I32, [P, P, P]),
         "rtBuildBvhNoAlloc": (I32, [P, U32, U32, P, P]),
+        "rtExportImage": (I32, [P, P, U32, U32, F32, P, P]),
         "rtgbGenCornell": (U32, [U64, U32, U32, F32, F32, F32, P, P, P]),
         "rtgbGenIcosphere": (U32, [U64, U32, F32, F32, U32, P]),
         "rtgbGenCameraRays": (None, [ctypes.POINTER(Camera), U32, U32, F32, F32, P]),
@@ -383,6 +384,20 @@ class Scene:
         self.ctx.check(LIB.rtTraceClosestHost(self.ctx.handle, self.id, _ptr(rays), len(rays), _ptr(hits)),
                        "rtTraceClosestHost")
         return hits
+
+
+def export_image(ctx: "Context", d_rgba32f, width: int, height: int, d_rgba8, gamma: float = 2.2, stream=None):
+    """RGBA32F device image -> gamma-encoded RGBA8 device image (rtExportImage)."""
+    ctx.check(LIB.rtExportImage(ctx.handle, _ptr(d_rgba32f), width, height, gamma, _ptr(d_rgba8), stream),
+              "rtExportImage")
+
+
+def write_ppm(path: str, rgba8: np.ndarray) -> None:
+    """Writes an (H, W, 4) uint8 image as a binary PPM (alpha dropped)."""
+    h, w = rgba8.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(rgba8[:, :, :3]).tobytes())
 
 
 def hits_view(hits: np.ndarray):
