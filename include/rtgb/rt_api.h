@@ -161,6 +161,12 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from 1024x1024 pixels up; images are
  *                   identical in every mode
+ *   "bvh.builder"   tree built by rtUploadScene when no nodes are given:
+ *                   0 (default) the reference's Bvh.h tree, node-for-node;
+ *                   1 a linear BVH over Morton-ordered centroids (not the
+ *                   reference's tree; hits are the same except where two
+ *                   triangles return the same t, and rtDownloadBvh returns
+ *                   this tree)
  * Values persist for the context; the autotuner (rtgb.autotune) writes
  * them. Unknown keys return RT_ERR_INVALID_ARGUMENT. */
 rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);

@@ -231,3 +231,37 @@ def test_tuning_keys(rt, ctx):
     with pytest.raises(rt.RtError):
         ctx.set_tuning("trace.refill", 0)
     assert 1 <= ctx.get_tuning("trace.refill") <= 32
+
+
+def test_lbvh_mode_same_hits(rt, orc, ctx):
+    """The separately reported LBVH tree: valid tree, every triangle in one
+    leaf, and the same closest hits as the reference tree (ties excepted)."""
+    tris = rt.gen_icosphere(5, 6)
+    mats = rt.gen_cornell(1, 0)[1]
+    ref_sc = ctx.upload_scene(tris, mats)
+    old = ctx.get_tuning("bvh.builder")
+    ctx.set_tuning("bvh.builder", 1)
+    try:
+        sc = ctx.upload_scene(tris, mats)
+    finally:
+        ctx.set_tuning("bvh.builder", old)
+    try:
+        nodes = sc.bvh()
+        objs = nodes.view(np.int32)[:, 9]
+        leaves = (nodes.view(np.int32)[:, 7] == -1)
+        assert sorted(objs[leaves].tolist()) == list(range(len(tris)))
+        # Every inner box contains its children's boxes.
+        inner = np.nonzero(~leaves)[0]
+        L, R = nodes.view(np.int32)[inner, 7], nodes.view(np.int32)[inner, 8]
+        for c in (L, R):
+            assert (nodes[inner][:, 0:3] <= nodes[c][:, 0:3]).all() and (nodes[inner][:, 4:7] >= nodes[c][:, 4:7]).all()
+        assert sc.info().depth <= 64
+        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 96, 96)
+        rays = np.concatenate([rt.gen_camera_rays(cam, 96, 96), rt.gen_random_rays(21, 20000)])
+        want, st = orc.trace(tris, ref_sc.bvh(), rays, stats=True)
+        ties = (st[:, 2] & 1) != 0
+        compare(gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32), want, ties)
+        compare(gpu_trace(ctx, ref_sc, rays, flags=rt.HIT_FP32), want, ties)
+    finally:
+        sc.release()
+        ref_sc.release()

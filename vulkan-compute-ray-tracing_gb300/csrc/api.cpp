@@ -51,6 +51,7 @@ struct rt_ctx {
   std::atomic<uint32_t> counter_slot{0};
   TraceOpts trace_opts;
   RenderOpts render_opts;
+  BuildOpts build_opts;
   uint64_t budget = 0, used = 0, tick = 0;
   // Device staging for rtTraceClosestHost (two chunk buffers per aux stream).
   void *stage[2] = {nullptr, nullptr};
@@ -413,11 +414,22 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   if (nodes) {
     UCK(cudaMemcpyAsync(dnodes, nodes, sizeof(rt_bvh_node) * nnodes, cudaMemcpyHostToDevice, st), "upload nodes");
   } else {
-    std::vector<uint8_t> axes(nnodes);
-    glibc_rand_axes(bvh_seed, nnodes, axes.data());
+    int builder = 0;
+    {
+      std::lock_guard<std::mutex> g(ctx->mu);
+      builder = ctx->build_opts.builder;
+    }
     char errbuf[256] = {0};
-    rt_status bs = gpu_build_bvh((const rt_triangle *)(slab + off_tris), nt, axes.data(), dnodes, st, &sc->build_ms,
-                                 &depth, errbuf, sizeof(errbuf));
+    rt_status bs;
+    if (builder == 1) {
+      bs = gpu_build_lbvh((const rt_triangle *)(slab + off_tris), nt, dnodes, st, &sc->build_ms, &depth, errbuf,
+                          sizeof(errbuf));
+    } else {
+      std::vector<uint8_t> axes(nnodes);
+      glibc_rand_axes(bvh_seed, nnodes, axes.data());
+      bs = gpu_build_bvh((const rt_triangle *)(slab + off_tris), nt, axes.data(), dnodes, st, &sc->build_ms, &depth,
+                         errbuf, sizeof(errbuf));
+    }
     if (bs != RT_SUCCESS) return abort_upload(fail(ctx, bs, "%s", errbuf));
   }
   d.depth = depth;
@@ -607,7 +619,8 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
   // Chunks alternate between two streams so the copy of one chunk overlaps
   // the traversal of the other.
   const uint32_t chunk = 1u << 20;
-  const size_t need = (size_t)chunk * (sizeof(rt_ray) + sizeof(rt_hit));
+  const size_t io_bytes = (size_t)chunk * (sizeof(rt_ray) + sizeof(rt_hit));
+  const size_t need = io_bytes + raysort_scratch_bytes(chunk);
   if (ctx->stage_bytes < need) {
     for (int i = 0; i < 2; i++) {
       if (ctx->stage[i]) cudaFree(ctx->stage[i]);
@@ -623,7 +636,10 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     rt_ray *dr = (rt_ray *)ctx->stage[s];
     rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
     CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
-    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st), "trace launch");
+    uint32_t *perm = nullptr;
+    if (opts.sort && m >= 65536)
+      CK(launch_raysort(dr, m, nullptr, (char *)ctx->stage[s] + io_bytes, &perm, st), "ray sort");
+    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm), "trace launch");
     CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
   }
   CK(cudaStreamSynchronize(ctx->aux[0]), "trace");
@@ -705,6 +721,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->render_opts.mode = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "bvh.builder") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->build_opts.builder = (int)value;
+    return RT_SUCCESS;
+  }
   ctx->last_error = "rtSetTuning: unknown key " + k;
   return RT_ERR_INVALID_ARGUMENT;
 }
@@ -723,6 +744,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "render.mode") {
     *value = ctx->render_opts.mode;
+    return RT_SUCCESS;
+  }
+  if (k == "bvh.builder") {
+    *value = ctx->build_opts.builder;
     return RT_SUCCESS;
   }
   return RT_ERR_INVALID_ARGUMENT;

@@ -97,6 +97,11 @@ struct RenderOpts {
   int mode = 2;  // 0 megakernel, 1 wavefront, 2 choose by image size
 };
 
+// Tree used when a scene is uploaded without nodes (rtSetTuning "bvh.builder").
+struct BuildOpts {
+  int builder = 0;  // 0 the reference's Bvh.h tree (bit-exact), 1 LBVH
+};
+
 // One job of a batched render (render.cu: k_render_batch).
 struct BatchJob {
   DevScene sc;
@@ -132,6 +137,12 @@ uint64_t ctx_budget(rt_ctx *ctx);
 int ctx_device(rt_ctx *ctx);
 // Device bytes rtUploadScene allocates for a scene of these counts.
 uint64_t scene_device_bytes(uint32_t n_triangles, uint32_t n_materials, uint32_t n_lights, uint32_t n_spheres);
+
+// ---------------------------------------------------------------- lbvh.cu
+// A linear BVH (Morton order) in the Bvh.h node layout; not the reference's
+// tree — a separately reported traversal mode.
+rt_status gpu_build_lbvh(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_nodes, cudaStream_t st, float *ms_out,
+                         uint32_t *depth_out, char *errbuf, size_t errlen);
 
 // ---------------------------------------------------------------- glibc_rand.cpp
 // glibc's TYPE_3 random() (what rand() returns) after srand(seed).
