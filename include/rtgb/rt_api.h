@@ -157,6 +157,10 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   order of origin and direction (hits still land at their
  *                   ray's input index; scratch comes from the stream-ordered
  *                   pool); also reorders each bounce of a wavefront render
+ *   "trace.packet"  1 (default) = a warp whose 32 rays share an origin and
+ *                   point within ~18 degrees traverses them as one packet
+ *                   (one node sequence, every lane busy); 0 = always one
+ *                   traversal per lane. Results are identical either way
  *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from 1024x1024 pixels up; images are

@@ -202,11 +202,13 @@ enum { FLAG_TIE = 1u, FLAG_TRUNCATED = 2u };
 // Closest hit over the reference node array.
 //   literal = true : hit_bvh exactly (comp:262-311): DFS that always pushes
 //                    left then right, no t-culling, a stack of `stack_size`
-//                    entries whose overflow ends the traversal.
+//                    entries whose overflow ends the traversal; among
+//                    candidates with exactly equal t the first met wins.
 //   literal = false: the same hit set with t-culling and near-first order
 //                    (unbounded stack); this is the cheapest exact traversal
 //                    of the reference tree in the reference layout, and its
 //                    record counts define the algorithmic bytes per ray.
+//                    Exactly equal t: the lower triangle index wins.
 // `slack` widens the cull window (tn > closest * (1 + slack)) so that every
 // candidate within the tie window is seen; slack = 0 counts records exactly.
 template <typename T>
@@ -225,7 +227,12 @@ bool trace_closest(const Scene &sc, V3<T> ro, V3<T> rd, T tmin, T tmax, bool lit
     // the tie tracker; acceptance below is the shader's `t < closest`.
     bool ok = hit_triangle(sc.tris[ti], ro, rd, tmin, tmax, tmp, &u, &v);
     if (!ok) return;
-    if (tmp.t < closest) {
+    // Exactly equal t: the shader keeps the first one its visiting order
+    // meets (comp:217); the literal traversal does that, the culled one
+    // resolves it by the lower triangle index so that the result does not
+    // depend on the order (the GPU kernels use the same rule).
+    bool better = tmp.t < closest || (!literal && hit && tmp.t == closest && ti < best_tri);
+    if (better) {
       if (hit) second = std::min(second, closest);
       hit = true;
       closest = tmp.t;

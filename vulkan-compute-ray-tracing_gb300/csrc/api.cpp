@@ -716,6 +716,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.sort = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.packet") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.packet = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.mode") {
     if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.mode = (int)value;
@@ -740,6 +745,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.sort") {
     *value = ctx->trace_opts.sort;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.packet") {
+    *value = ctx->trace_opts.packet;
     return RT_SUCCESS;
   }
   if (k == "render.mode") {

@@ -60,6 +60,7 @@ cudaError_t launch_relayout(const rt_bvh_node *nodes, uint32_t nnodes, const rt_
 struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
   int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
+  int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
 };
 
 // `counter` is a device word private to this launch (work distribution);

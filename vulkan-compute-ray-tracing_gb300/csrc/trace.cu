@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
         }
       }
       if (node != kDone) {
-        test_triangle(sc.tpre, ~node, r, closest, best, bu, bv);
+        test_triangle(sc.tpre, sc.leaf_tri, ~node, r, closest, best, bu, bv);
         node = sp > 0 ? stack[--sp] : kDone;
       }
       if (node == kDone) {
@@ -149,29 +149,43 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
   }
 }
 
-// Whole-warp batches: a warp claims 32 consecutive rays and each lane runs
-// its ray to completion in a tight loop. Consecutive rays of a camera are
-// neighbours on screen, so the lanes of a warp walk similar parts of the
-// tree; this is the faster form for coherent batches.
+// Whole-warp batches: a warp claims 32 consecutive rays (consecutive in
+// Morton order when the batch was reordered). If they share an origin and
+// point the same way (a camera tile), the warp traverses them as one packet
+// (traverse_packet: every lane busy, ~1.5x the nodes of a single ray);
+// otherwise each lane runs its own ray to completion in a tight loop.
 template <int STACK, bool REFINE>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(DevScene sc, const float4 *__restrict__ rays,
                                                              uint32_t n, int4 *__restrict__ hits,
                                                              uint32_t *__restrict__ counter, uint32_t *err,
-                                                             const uint32_t *__restrict__ perm) {
-  const uint32_t lane = threadIdx.x & 31;
+                                                             const uint32_t *__restrict__ perm, int packet) {
+  __shared__ int s_stack[kTraceBlock / 32][STACK];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(counter, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) return;
     uint32_t i = base + lane;
-    if (i < n) {
+    const bool active = i < n;
+    f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
+    float tmin = 0.0f, tmax = 0.0f;
+    if (active) {
       if (perm) i = __ldg(perm + i);
       float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
-      f3 o = mk3(r0.x, r0.y, r0.z), d = mk3(r1.x, r1.y, r1.z);
-      TraceRay r = make_ray(o, d, r0.w);
-      float closest = r1.w, u = 0.0f, v = 0.0f;
-      int k = traverse_closest<STACK>(sc, r, closest, u, v, err);
+      o = mk3(r0.x, r0.y, r0.z);
+      d = mk3(r1.x, r1.y, r1.z);
+      tmin = r0.w;
+      tmax = r1.w;
+    }
+    TraceRay r = make_ray(o, d, tmin);
+    float closest = tmax, u = 0.0f, v = 0.0f;
+    int k;
+    if (packet && warp_is_coherent(active, r))
+      k = traverse_packet<STACK>(sc, r, active, closest, u, v, s_stack[warp], err);
+    else
+      k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
+    if (active) {
       int4 h;
       if (k >= 0) {
         int tri = __ldg(sc.leaf_tri + k);
@@ -214,7 +228,8 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
   if (grid > want) grid = want;
   if (batch)
     k_trace_batch<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                               reinterpret_cast<int4 *>(hits), counter, err, perm);
+                                                               reinterpret_cast<int4 *>(hits), counter, err, perm,
+                                                               opts.packet);
   else
     k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
                                                          reinterpret_cast<int4 *>(hits), counter, err, opts.refill,

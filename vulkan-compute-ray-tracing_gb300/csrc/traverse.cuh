@@ -8,8 +8,9 @@
 // tNear <= tFar, comp:286) and the nearer child is visited first. Pruning
 // never skips a box that holds a closer accepted hit, because every box is
 // the union of its triangles' boxes padded by 1e-4 (Bvh.h:94-98); so the hit
-// index and t equal the reference's except when two triangles return the
-// same t, where "first found" depends on the visiting order.
+// index and t equal the reference's except when two triangles return exactly
+// the same t: the reference keeps the first one its order meets, here the
+// lower triangle index wins (test_triangle), which no order or tree changes.
 #pragma once
 #include "rt_internal.h"
 #include "rt_math.cuh"
@@ -56,8 +57,15 @@ __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float h
 
 // triIntersect on a precomputed record; updates (closest, best, u, v) when
 // the triangle is accepted. Bit-exact with the fp32 evaluation of comp:157-173.
-__device__ __forceinline__ void test_triangle(const float4 *__restrict__ tpre, int k, const TraceRay &r,
-                                              float &closest, int &best, float &bu, float &bv) {
+// Acceptance is the shader's tmin < t < closest, except that a triangle at
+// exactly the current closest t replaces the current one when its triangle
+// index is lower: the reference keeps whichever equal-t triangle its
+// visiting order meets first, which makes the winner depend on the order
+// (and on the tree); with this rule every traversal order, ray ordering and
+// tree returns the same triangle. The index loads happen only on exact ties.
+__device__ __forceinline__ void test_triangle(const float4 *__restrict__ tpre, const int32_t *__restrict__ leaf_tri,
+                                              int k, const TraceRay &r, float &closest, int &best, float &bu,
+                                              float &bv) {
   const float4 *T = tpre + 3ll * k;
   float4 t0 = __ldg(T), t1 = __ldg(T + 1), t2 = __ldg(T + 2);
   f3 v0 = mk3(t0.x, t0.y, t0.z), n = mk3(t0.w, t1.x, t1.y);
@@ -65,7 +73,8 @@ __device__ __forceinline__ void test_triangle(const float4 *__restrict__ tpre, i
   f3 p = sub3(v0, r.o);
   float idet = __fdiv_rn(1.0f, dot3(r.d, n));
   float t = __fmul_rn(dot3(n, p), idet);
-  if (t > r.tmin && t < closest) {
+  if (t > r.tmin &&
+      (t < closest || (t == closest && best >= 0 && __ldg(leaf_tri + k) < __ldg(leaf_tri + best)))) {
     f3 q = cross3(p, r.d);
     float u = __fmul_rn(dot3(q, b), idet);
     float v = __fmul_rn(dot3(q, a), idet);
@@ -119,10 +128,88 @@ __device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceR
         node = stack[--sp];
       }
     }
-    test_triangle(sc.tpre, ~node, r, closest, best, bu, bv);
+    test_triangle(sc.tpre, sc.leaf_tri, ~node, r, closest, best, bu, bv);
     if (sp == 0) return best;
     node = stack[--sp];
   }
+}
+
+// Warp-wide packet traversal for 32 coherent rays: the warp walks one node
+// sequence with one stack (in shared memory, written by lane 0), descending
+// into a child when ANY active lane's box test passes with that lane's own
+// closest t; every active lane then tests each reached leaf's triangle
+// against its own ray. Each lane's result is exactly its per-ray closest hit
+// (the packet visits a superset of every lane's required nodes); only the
+// number of visited nodes changes. Near/far order follows the majority of
+// the lanes that hit both children. All branches are warp-uniform except the
+// triangle test.
+template <int STACK>
+__device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRay &r, bool active, float &closest,
+                                               float &bu, float &bv, volatile int *stack, uint32_t *err) {
+  const uint32_t lane = threadIdx.x & 31;
+  const float INF = __int_as_float(0x7f800000);
+  int best = -1;
+  float root = active ? slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1], sc.root_lo[2],
+                                   sc.root_hi[2], closest)
+                      : INF;
+  if (!__any_sync(0xffffffffu, root < INF)) return -1;
+  int sp = 0;
+  int node = sc.root_ref;
+  const float4 *__restrict__ bvh = sc.bvh2;
+  for (;;) {
+    if (node >= 0) {
+      const float4 *N = bvh + 4ll * node;
+      float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
+      float t0 = active ? slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest) : INF;
+      float t1 = active ? slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest) : INF;
+      const bool h0 = t0 < INF, h1 = t1 < INF;
+      const uint32_t m0 = __ballot_sync(0xffffffffu, h0), m1 = __ballot_sync(0xffffffffu, h1);
+      const int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+      if (m0 && m1) {
+        const uint32_t pref0 = __ballot_sync(0xffffffffu, h0 && (!h1 || t0 <= t1));
+        const uint32_t pref1 = __ballot_sync(0xffffffffu, h1 && (!h0 || t1 < t0));
+        const bool first0 = __popc(pref0) >= __popc(pref1);
+        if (sp >= STACK) {
+          if (lane == 0) atomicOr(err, KERR_STACK_OVERFLOW);
+          return best;
+        }
+        if (lane == 0) stack[sp] = first0 ? r1 : r0;
+        __syncwarp();
+        sp++;
+        node = first0 ? r0 : r1;
+      } else if (m0) {
+        node = r0;
+      } else if (m1) {
+        node = r1;
+      } else {
+        if (sp == 0) return best;
+        node = stack[--sp];
+      }
+    } else {
+      if (active) test_triangle(sc.tpre, sc.leaf_tri, ~node, r, closest, best, bu, bv);
+      if (sp == 0) return best;
+      node = stack[--sp];
+    }
+  }
+}
+
+// True when the warp's 32 rays suit packet traversal: active lanes share one
+// origin and all directions lie within ~18 degrees of the first active one.
+__device__ __forceinline__ bool warp_is_coherent(bool active, const TraceRay &r) {
+  const uint32_t act = __ballot_sync(0xffffffffu, active);
+  if (act == 0) return false;
+  const int src = __ffs(act) - 1;
+  float ox = __shfl_sync(0xffffffffu, r.o.x, src), oy = __shfl_sync(0xffffffffu, r.o.y, src);
+  float oz = __shfl_sync(0xffffffffu, r.o.z, src);
+  float dx = __shfl_sync(0xffffffffu, r.d.x, src), dy = __shfl_sync(0xffffffffu, r.d.y, src);
+  float dz = __shfl_sync(0xffffffffu, r.d.z, src);
+  bool ok = true;
+  if (active) {
+    float dd = r.d.x * dx + r.d.y * dy + r.d.z * dz;
+    float n0 = dx * dx + dy * dy + dz * dz, n1 = r.d.x * r.d.x + r.d.y * r.d.y + r.d.z * r.d.z;
+    ok = r.o.x == ox && r.o.y == oy && r.o.z == oz && dd > 0.95f * sqrtf(n0 * n1);
+  }
+  return __all_sync(0xffffffffu, ok);
 }
 
 }  // namespace rtgb
