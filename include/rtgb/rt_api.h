@@ -161,16 +161,20 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   point within ~18 degrees traverses them as one packet
  *                   (one node sequence, every lane busy); 0 = always one
  *                   traversal per lane. Results are identical either way
+ *   "trace.smem"    1 = per-lane traversal stacks in shared memory instead
+ *                   of registers/local memory (0, default); same results
  *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from 1024x1024 pixels up; images are
  *                   identical in every mode
  *   "bvh.builder"   tree built by rtUploadScene when no nodes are given:
  *                   0 (default) the reference's Bvh.h tree, node-for-node;
- *                   1 a linear BVH over Morton-ordered centroids (not the
- *                   reference's tree; hits are the same except where two
- *                   triangles return the same t, and rtDownloadBvh returns
- *                   this tree)
+ *                   1 a linear BVH over Morton-ordered centroids,
+ *                   2 agglomerative clustering of Morton-ordered triangles
+ *                   (PLOC; tighter boxes, slower build). 1 and 2 are not
+ *                   the reference's tree, but closest hits are identical
+ *                   (equal-t ties go to the lower triangle index in every
+ *                   tree); rtDownloadBvh returns the tree that was built
  * Values persist for the context; the autotuner (rtgb.autotune) writes
  * them. Unknown keys return RT_ERR_INVALID_ARGUMENT. */
 rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);

@@ -240,14 +240,15 @@ def test_tuning_keys(rt, ctx):
     assert 1 <= ctx.get_tuning("trace.refill") <= 32
 
 
-def test_lbvh_mode_same_hits(rt, orc, ctx):
-    """The separately reported LBVH tree: valid tree, every triangle in one
-    leaf, and the same closest hits as the reference tree (ties excepted)."""
+@pytest.mark.parametrize("builder", [1, 2], ids=["lbvh", "ploc"])
+def test_alt_tree_mode_same_hits(rt, orc, ctx, builder):
+    """The separately reported trees (1 LBVH, 2 PLOC): valid tree, every
+    triangle in one leaf, and the same closest hits as the reference tree."""
     tris = rt.gen_icosphere(5, 6)
     mats = rt.gen_cornell(1, 0)[1]
     ref_sc = ctx.upload_scene(tris, mats)
     old = ctx.get_tuning("bvh.builder")
-    ctx.set_tuning("bvh.builder", 1)
+    ctx.set_tuning("bvh.builder", builder)
     try:
         sc = ctx.upload_scene(tris, mats)
     finally:

@@ -424,6 +424,9 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
     if (builder == 1) {
       bs = gpu_build_lbvh((const rt_triangle *)(slab + off_tris), nt, dnodes, st, &sc->build_ms, &depth, errbuf,
                           sizeof(errbuf));
+    } else if (builder == 2) {
+      bs = gpu_build_ploc((const rt_triangle *)(slab + off_tris), nt, dnodes, st, &sc->build_ms, &depth, errbuf,
+                          sizeof(errbuf));
     } else {
       std::vector<uint8_t> axes(nnodes);
       glibc_rand_axes(bvh_seed, nnodes, axes.data());
@@ -721,13 +724,18 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.packet = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.smem") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.smem = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.mode") {
     if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.mode = (int)value;
     return RT_SUCCESS;
   }
   if (k == "bvh.builder") {
-    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
     ctx->build_opts.builder = (int)value;
     return RT_SUCCESS;
   }
@@ -749,6 +757,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.packet") {
     *value = ctx->trace_opts.packet;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.smem") {
+    *value = ctx->trace_opts.smem;
     return RT_SUCCESS;
   }
   if (k == "render.mode") {

@@ -219,17 +219,49 @@ __global__ void k_lbvh_boxes(const rt_triangle *__restrict__ tris, const uint32_
 
 }  // namespace
 
+size_t lbvh_sorted_keys_words(uint32_t n) { return 16 + 6ull * n + (n / 1024 + 8); }
+
+// Centroid bounds -> Morton codes -> stable radix sort. `scratch` holds
+// lbvh_sorted_keys_words(n) words: bounds 16 | codes 2n | indices 2n |
+// flags n | scan n | scan block sums n/1024+8. The sorted codes and triangle
+// indices are returned as pointers into it.
+cudaError_t lbvh_sorted_keys(const rt_triangle *d_tris, uint32_t n, uint32_t *scratch, uint32_t **codes_out,
+                             uint32_t **idx_out, cudaStream_t st) {
+  uint32_t *ext = scratch;
+  uint32_t *codes[2] = {ext + 16, ext + 16 + n};
+  uint32_t *idx[2] = {ext + 16 + 2ull * n, ext + 16 + 3ull * n};
+  uint32_t *flag = ext + 16 + 4ull * n;
+  uint32_t *pos = flag + n;
+  uint32_t *sums = pos + n;
+  const uint32_t B = 256, G = (n + B - 1) / B;
+  k_init_bounds<<<1, 32, 0, st>>>(ext);
+  k_bounds<<<304, 256, 0, st>>>(d_tris, n, ext);
+  k_morton<<<G, B, 0, st>>>(d_tris, n, ext, codes[0], idx[0]);
+  int cur = 0;
+  cudaError_t e = cudaSuccess;
+  for (int bit = 0; bit < 30; bit++) {
+    k_bitflag<<<G, B, 0, st>>>(codes[cur], n, bit, flag);
+    e = exclusive_scan_u32(flag, pos, sums, n, st);
+    if (e != cudaSuccess) return e;
+    k_split<<<G, B, 0, st>>>(codes[cur], idx[cur], flag, pos, n, codes[cur ^ 1], idx[cur ^ 1]);
+    cur ^= 1;
+  }
+  *codes_out = codes[cur];
+  *idx_out = idx[cur];
+  return cudaGetLastError();
+}
+
 rt_status gpu_build_lbvh(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_nodes, cudaStream_t st, float *ms_out,
                          uint32_t *depth_out, char *errbuf, size_t errlen) {
   if (n == 0) return RT_ERR_INVALID_ARGUMENT;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  // Scratch, in 32-bit words: bounds 16 | codes 2n | indices 2n | flags n |
-  // scan n | scan block sums n/1024+8 | left n | right n | parent 2n |
-  // visit counts n | depth 8.
+  // Scratch, in 32-bit words: the sort's words | left n | right n |
+  // parent 2n | visit counts n | depth 8.
   void *mem = nullptr;
-  const size_t words = 16 + 2ull * n + 2ull * n + n + n + (n / 1024 + 8) + n + n + 2ull * n + n + 8;
+  const size_t sort_words = lbvh_sorted_keys_words(n);
+  const size_t words = sort_words + n + n + 2ull * n + n + 8;
   cudaError_t e = cudaMallocAsync(&mem, 4 * words, st);
   if (e != cudaSuccess) {
     std::snprintf(errbuf, errlen, "lbvh scratch: %s", cudaGetErrorString(e));
@@ -237,34 +269,22 @@ rt_status gpu_build_lbvh(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_n
     cudaEventDestroy(e1);
     return RT_ERR_OUT_OF_MEMORY;
   }
-  uint32_t *ext = static_cast<uint32_t *>(mem);
-  uint32_t *codes[2] = {ext + 16, ext + 16 + n};
-  uint32_t *idx[2] = {ext + 16 + 2ull * n, ext + 16 + 3ull * n};
-  uint32_t *flag = ext + 16 + 4ull * n;
-  uint32_t *pos = flag + n;
-  uint32_t *sums = pos + n;
-  int32_t *left = reinterpret_cast<int32_t *>(sums + n / 1024 + 8);
+  uint32_t *sortbuf = static_cast<uint32_t *>(mem);
+  int32_t *left = reinterpret_cast<int32_t *>(sortbuf + sort_words);
   int32_t *right = left + n;
   int32_t *parent = right + n;
   uint32_t *visits = reinterpret_cast<uint32_t *>(parent + 2ull * n);
   uint32_t *dmax = visits + n;
   cudaEventRecord(e0, st);
   const uint32_t B = 256, G = (n + B - 1) / B;
-  k_init_bounds<<<1, 32, 0, st>>>(ext);
-  k_bounds<<<304, 256, 0, st>>>(d_tris, n, ext);
-  k_morton<<<G, B, 0, st>>>(d_tris, n, ext, codes[0], idx[0]);
-  int cur = 0;
-  for (int bit = 0; bit < 30; bit++) {
-    k_bitflag<<<G, B, 0, st>>>(codes[cur], n, bit, flag);
-    e = exclusive_scan_u32(flag, pos, sums, n, st);
-    if (e != cudaSuccess) break;
-    k_split<<<G, B, 0, st>>>(codes[cur], idx[cur], flag, pos, n, codes[cur ^ 1], idx[cur ^ 1]);
-    cur ^= 1;
+  uint32_t *codes = nullptr, *idx = nullptr;
+  e = lbvh_sorted_keys(d_tris, n, sortbuf, &codes, &idx, st);
+  if (e == cudaSuccess) {
+    cudaMemsetAsync(visits, 0, 4ull * n + 32, st);  // visit counts and the depth word
+    cudaMemsetAsync(parent, 0xff, 4ull * 2 * n, st);
+    if (n > 1) k_karras<<<(n - 1 + B - 1) / B, B, 0, st>>>(codes, (int)n, left, right, parent);
+    k_lbvh_boxes<<<G, B, 0, st>>>(d_tris, idx, (int)n, left, right, parent, visits, d_nodes, dmax);
   }
-  cudaMemsetAsync(visits, 0, 4ull * n + 32, st);  // visit counts and the depth word
-  cudaMemsetAsync(parent, 0xff, 4ull * 2 * n, st);
-  if (n > 1) k_karras<<<(n - 1 + B - 1) / B, B, 0, st>>>(codes[cur], (int)n, left, right, parent);
-  k_lbvh_boxes<<<G, B, 0, st>>>(d_tris, idx[cur], (int)n, left, right, parent, visits, d_nodes, dmax);
   cudaEventRecord(e1, st);
   uint32_t depth = 0;
   cudaMemcpyAsync(&depth, dmax, 4, cudaMemcpyDeviceToHost, st);

@@ -61,6 +61,7 @@ struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
   int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
+  int smem = 0;     // 1: per-lane traversal stacks in shared memory instead of local memory
 };
 
 // `counter` is a device word private to this launch (work distribution);
@@ -100,7 +101,7 @@ struct RenderOpts {
 
 // Tree used when a scene is uploaded without nodes (rtSetTuning "bvh.builder").
 struct BuildOpts {
-  int builder = 0;  // 0 the reference's Bvh.h tree (bit-exact), 1 LBVH
+  int builder = 0;  // 0 the reference's Bvh.h tree (bit-exact), 1 LBVH, 2 PLOC
 };
 
 // One job of a batched render (render.cu: k_render_batch).
@@ -143,6 +144,13 @@ uint64_t scene_device_bytes(uint32_t n_triangles, uint32_t n_materials, uint32_t
 // A linear BVH (Morton order) in the Bvh.h node layout; not the reference's
 // tree — a separately reported traversal mode.
 rt_status gpu_build_lbvh(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_nodes, cudaStream_t st, float *ms_out,
+                         uint32_t *depth_out, char *errbuf, size_t errlen);
+// Morton-sorted triangle centroids (lbvh.cu), shared by the LBVH and PLOC builders.
+size_t lbvh_sorted_keys_words(uint32_t n);
+cudaError_t lbvh_sorted_keys(const rt_triangle *d_tris, uint32_t n, uint32_t *scratch, uint32_t **codes_out,
+                             uint32_t **idx_out, cudaStream_t st);
+// Agglomerative-clustering tree (ploc.cu), Bvh.h node layout, root node 0.
+rt_status gpu_build_ploc(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_nodes, cudaStream_t st, float *ms_out,
                          uint32_t *depth_out, char *errbuf, size_t errlen);
 
 // ---------------------------------------------------------------- glibc_rand.cpp

@@ -154,12 +154,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
 // point the same way (a camera tile), the warp traverses them as one packet
 // (traverse_packet: every lane busy, ~1.5x the nodes of a single ray);
 // otherwise each lane runs its own ray to completion in a tight loop.
-template <int STACK, bool REFINE>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_batch(DevScene sc, const float4 *__restrict__ rays,
+template <int STACK, bool REFINE, bool SMEM>
+__global__ void __launch_bounds__(kTraceBlock, SMEM ? 8 : 16) k_trace_batch(DevScene sc, const float4 *__restrict__ rays,
                                                              uint32_t n, int4 *__restrict__ hits,
                                                              uint32_t *__restrict__ counter, uint32_t *err,
                                                              const uint32_t *__restrict__ perm, int packet) {
   __shared__ int s_stack[kTraceBlock / 32][STACK];
+  // Per-lane traversal stacks in shared memory, one column per thread.
+  __shared__ int s_lane[SMEM ? STACK * kTraceBlock : 1];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     uint32_t base = 0;
@@ -183,6 +185,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(DevScene sc, const 
     int k;
     if (packet && warp_is_coherent(active, r))
       k = traverse_packet<STACK>(sc, r, active, closest, u, v, s_stack[warp], err);
+    else if (SMEM)
+      k = active ? traverse_closest_on<STACK>(sc, r, closest, u, v, err, s_lane + threadIdx.x, kTraceBlock) : -1;
     else
       k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
     if (active) {
@@ -218,18 +222,24 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
                            uint32_t *err, const TraceOpts &opts, const uint32_t *perm, cudaStream_t st) {
   const bool batch = opts.refill >= 32;
   int blocks_per_sm = 0;
-  if (batch)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_batch<STACK, REFINE>, kTraceBlock, 0);
+  if (batch && opts.smem)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_batch<STACK, REFINE, true>, kTraceBlock, 0);
+  else if (batch)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_batch<STACK, REFINE, false>, kTraceBlock, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<STACK, REFINE>, kTraceBlock, 0);
   if (blocks_per_sm < 1) blocks_per_sm = 1;
   uint32_t want = (n + kTraceBlock - 1) / kTraceBlock;
   uint32_t grid = (uint32_t)(g_num_sms * blocks_per_sm);
   if (grid > want) grid = want;
-  if (batch)
-    k_trace_batch<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                               reinterpret_cast<int4 *>(hits), counter, err, perm,
-                                                               opts.packet);
+  if (batch && opts.smem)
+    k_trace_batch<STACK, REFINE, true><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
+                                                                     reinterpret_cast<int4 *>(hits), counter, err,
+                                                                     perm, opts.packet);
+  else if (batch)
+    k_trace_batch<STACK, REFINE, false><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
+                                                                      reinterpret_cast<int4 *>(hits), counter, err,
+                                                                      perm, opts.packet);
   else
     k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
                                                          reinterpret_cast<int4 *>(hits), counter, err, opts.refill,

@@ -43,6 +43,19 @@ __device__ __forceinline__ TraceRay make_ray(f3 o, f3 d, float tmin) {
   return r;
 }
 
+// Three-operand fp32 min/max (sm_100 and later), NaN operands ignored as
+// with fminf/fmaxf.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Slab test of [lo, hi] against [tmin, tmax]; returns the entry distance or
 // +inf when the box is missed.
 __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float hx, float ly, float hy, float lz,
@@ -50,8 +63,8 @@ __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float h
   float ax = fmaf(lx, r.ix, -r.ox), bx = fmaf(hx, r.ix, -r.ox);
   float ay = fmaf(ly, r.iy, -r.oy), by = fmaf(hy, r.iy, -r.oy);
   float az = fmaf(lz, r.iz, -r.oz), bz = fmaf(hz, r.iz, -r.oz);
-  float tn = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), r.tmin));
-  float tf = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fminf(fmaxf(az, bz), tmax));
+  float tn = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), r.tmin));
+  float tf = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
 
@@ -88,14 +101,16 @@ __device__ __forceinline__ void test_triangle(const float4 *__restrict__ tpre, c
 }
 
 // Returns the leaf index (position in tpre) of the closest hit or -1.
+// The traversal stack is stack[i * stride] for i < STACK: a per-thread local
+// array (stride 1) or a column of a shared-memory block (stride = threads
+// per block, so each lane keeps to its own bank).
 template <int STACK>
-__device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceRay &r, float &closest, float &bu,
-                                                float &bv, uint32_t *err) {
+__device__ __forceinline__ int traverse_closest_on(const DevScene &sc, const TraceRay &r, float &closest, float &bu,
+                                                   float &bv, uint32_t *err, int *stack, int stride) {
   int best = -1;
   float root = slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1], sc.root_lo[2],
                           sc.root_hi[2], closest);
   if (!(root < __int_as_float(0x7f800000))) return -1;
-  int stack[STACK];
   int sp = 0;
   int node = sc.root_ref;
   const float4 *__restrict__ bvh = sc.bvh2;
@@ -117,7 +132,7 @@ __device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceR
           atomicOr(err, KERR_STACK_OVERFLOW);
           return best;
         }
-        stack[sp++] = farc;
+        stack[(sp++) * stride] = farc;
         node = nearc;
       } else if (h0) {
         node = r0;
@@ -125,13 +140,20 @@ __device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceR
         node = r1;
       } else {
         if (sp == 0) return best;
-        node = stack[--sp];
+        node = stack[(--sp) * stride];
       }
     }
     test_triangle(sc.tpre, sc.leaf_tri, ~node, r, closest, best, bu, bv);
     if (sp == 0) return best;
-    node = stack[--sp];
+    node = stack[(--sp) * stride];
   }
+}
+
+template <int STACK>
+__device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceRay &r, float &closest, float &bu,
+                                                float &bv, uint32_t *err) {
+  int stack[STACK];
+  return traverse_closest_on<STACK>(sc, r, closest, bu, bv, err, stack, 1);
 }
 
 // Warp-wide packet traversal for 32 coherent rays: the warp walks one node
