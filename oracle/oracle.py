@@ -62,6 +62,73 @@ def ref_available() -> bool:
     return os.path.exists(REF_PATH)
 
 
+REF_SCENE_DIR = os.path.join(HERE, "_ref", "doge_scene")
+
+
+def ref_scene_available() -> bool:
+    """True where the recipe copied the reference's demo-scene OBJ files."""
+    return os.path.exists(os.path.join(REF_SCENE_DIR, "buff-doge.obj"))
+
+
+def obj_triangles(path: str, material: int = 0) -> np.ndarray:
+    """Restatement of the reference's OBJ-to-triangles step
+    (src/scene/mesh.cpp:96-139 through tinyobjloader, then
+    src/ray-tracing/RtScene.h:13-31): every face's vertex positions in file
+    order, polygons fanned from their first vertex. Coordinates go through
+    Python's correctly rounded float() and then to float32; the reference
+    scene's six-decimal coordinates round the same way through any parser
+    that is accurate to double precision."""
+    verts, out = [], []
+    with open(path, "rb") as f:
+        text = f.read().decode("latin-1")
+    for line in text.replace("\r\n", "\n").replace("\r", "\n").split("\n"):
+        tok = line.split()
+        if not tok:
+            continue
+        if tok[0] == "v":
+            xyz = []
+            for t in tok[1:4]:
+                try:
+                    xyz.append(float(t))
+                except ValueError:
+                    xyz.append(0.0)
+            verts.append((xyz + [0.0, 0.0, 0.0])[:3])
+        elif tok[0] == "f":
+            ids = []
+            for t in tok[1:]:
+                i = int(t.split("/")[0])
+                if i == 0:
+                    raise ValueError("face index 0")
+                v = i - 1 if i > 0 else len(verts) + i
+                if not 0 <= v < len(verts):
+                    raise ValueError("face index out of range")
+                ids.append(v)
+            for k in range(1, len(ids) - 1):
+                row = np.zeros(12, np.float32)
+                for j, v in enumerate((ids[0], ids[k], ids[k + 1])):
+                    row[4 * j:4 * j + 3] = np.asarray(verts[v], np.float64).astype(np.float32)
+                row[11] = np.array([material], np.uint32).view(np.float32)[0]
+                out.append(row)
+    return np.array(out, np.float32).reshape(-1, 12)
+
+
+def reference_scene(model_dir: str):
+    """Restatement of GpuModel::Scene() (src/ray-tracing/RtScene.h:44-101):
+    (tris, mats, spheres) as float32 word arrays."""
+    objs = [("buff-doge.obj", 0), ("cheems.obj", 0), ("right.obj", 1), ("left.obj", 2), ("back.obj", 0),
+            ("ceil.obj", 0), ("floor.obj", 0), ("light.obj", 3)]
+    tris = np.concatenate([obj_triangles(os.path.join(model_dir, f), m) for f, m in objs])
+    mats = np.zeros((6, 8), np.float32)
+    for i, (typ, alb) in enumerate([(1, (0.3, 0.3, 0.3)), (1, (0.9, 0.1, 0.1)), (1, (0.1, 0.9, 0.1)),
+                                    (0, (2.0, 2.0, 2.0)), (2, (1.0, 1.0, 1.0)), (3, (1.0, 1.0, 1.0))]):
+        mats[i, 0] = np.array([typ], np.uint32).view(np.float32)[0]
+        mats[i, 4:7] = alb
+    sph = np.zeros((1, 8), np.float32)
+    sph[0, :4] = (0.6, 1.0, -1.0, 0.6)
+    sph[0, 4] = np.array([5], np.uint32).view(np.float32)[0]
+    return tris, mats, sph
+
+
 def ref_lib():
     lib = ctypes.CDLL(REF_PATH)
     lib.ref_create_bvh.restype = ctypes.c_int

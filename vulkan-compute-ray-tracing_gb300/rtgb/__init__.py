@@ -128,6 +128,9 @@ def _load() -> ctypes.CDLL:
         "rtgbGenGrid": (U32, [U64, U32, U32, U32, F32, F32, U32, F32, P, P]),
         "rtgbUniform": (ctypes.c_double, [U64, U64]),
         "rtgbGlibcRand": (None, [U32, U64, P]),
+        "rtLoadObj": (I32, [ctypes.c_char_p, U32, P, U32, ctypes.POINTER(U32)]),
+        "rtObjLastError": (ctypes.c_char_p, []),
+        "rtLoadReferenceScene": (I32, [ctypes.c_char_p, P, U32, ctypes.POINTER(U32), P, P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -215,6 +218,44 @@ def gen_random_rays(seed: int, n: int, lo: float = -1.5, hi: float = 1.5, tmin: 
     rays = np.zeros((n, RAY_WORDS), np.float32)
     LIB.rtgbGenRandomRays(seed, n, lo, hi, tmin, tmax, _ptr(rays))
     return rays
+
+
+def load_obj(path: str, material: int = 0) -> np.ndarray:
+    """Triangles of one OBJ file, all with `material` (GpuModel::getTriangles,
+    src/ray-tracing/RtScene.h:13-31). Raises RtError on a missing file or a
+    bad face index."""
+    n = ctypes.c_uint32()
+    st = LIB.rtLoadObj(os.fsencode(path), material, None, 0, ctypes.byref(n))
+    if st:
+        raise RtError(st, LIB.rtObjLastError().decode())
+    tris = np.zeros((max(n.value, 1), TRIANGLE_WORDS), np.float32)
+    st = LIB.rtLoadObj(os.fsencode(path), material, _ptr(tris), n.value, ctypes.byref(n))
+    if st:
+        raise RtError(st, LIB.rtObjLastError().decode())
+    return tris[:n.value]
+
+
+def load_reference_scene(model_dir: str):
+    """The reference's doge scene (src/ray-tracing/RtScene.h:44-101) from the
+    directory holding its OBJ files. Returns (tris, mats, spheres); lights
+    are derived by upload_scene (or lights_from_materials)."""
+    n = ctypes.c_uint32()
+    st = LIB.rtLoadReferenceScene(os.fsencode(model_dir), None, 0, ctypes.byref(n), None, None)
+    if st:
+        raise RtError(st, LIB.rtObjLastError().decode())
+    tris = np.zeros((max(n.value, 1), TRIANGLE_WORDS), np.float32)
+    mats = np.zeros((6, MATERIAL_WORDS), np.float32)
+    sph = np.zeros((1, SPHERE_WORDS), np.float32)
+    st = LIB.rtLoadReferenceScene(os.fsencode(model_dir), _ptr(tris), n.value, ctypes.byref(n), _ptr(mats),
+                                  _ptr(sph))
+    if st:
+        raise RtError(st, LIB.rtObjLastError().decode())
+    return tris[:n.value], mats, sph
+
+
+# The reference's starting camera position (src/main.cpp:37), for
+# camera_from_reference.
+REFERENCE_CAMERA_POS = (1.8, 8.6, 1.1)
 
 
 def lights_from_materials(tris: np.ndarray, mats: np.ndarray) -> np.ndarray:
