@@ -306,8 +306,9 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_step * 32,
                 "d2h_bytes_per_step": rays_step * 16, "matches_device_path": bool(same)},
         # Per batch: 7 reordering kernels (extent, histogram, 3-kernel scan,
-        # scatter, init) + 1 casting kernel; two batches per step.
-        "gpu_launches": 16 * args.steps,
+        # scatter, init) + 2 casting kernels (packets, then the listed
+        # chunks per lane); two batches per step.
+        "gpu_launches": 18 * args.steps,
         "clocks": clk.summary(),
     }
     # Separately reported: the same workload on trees that are not the

@@ -161,8 +161,17 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   point within ~18 degrees traverses them as one packet
  *                   (one node sequence, every lane busy); 0 = always one
  *                   traversal per lane. Results are identical either way
- *   "trace.smem"    1 = per-lane traversal stacks in shared memory instead
- *                   of registers/local memory (0, default); same results
+ *   "trace.spec"    1 (default) = per-lane traversal parks the first leaf it
+ *                   reaches and keeps descending until every lane of the
+ *                   warp holds one, then tests them together; 0 = test each
+ *                   leaf when reached. Results are identical either way
+ *   "trace.minblocks" 16, 12 (default) or 10: resident 128-thread blocks per
+ *                   SM the per-lane caster is compiled for (register budget)
+ *   "trace.packet_minblocks"  the same for the packet caster (default 16)
+ *   "trace.defer"   1 (default) = 32-ray chunks that fail the packet test are
+ *                   listed and cast by a second, per-lane kernel; 0 = cast
+ *                   in place by the packet kernel with plain per-lane
+ *                   traversal (no postponed leaves)
  *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from 1024x1024 pixels up; images are

@@ -201,34 +201,58 @@ def test_invalid_scenes_are_rejected(rt, ctx):
     sc.release()
 
 
-@pytest.mark.parametrize("refill,sort,packet", [(1, 0, 0), (4, 0, 0), (16, 0, 0), (32, 0, 0), (32, 1, 0), (4, 1, 0),
-                                                (32, 1, 1), (32, 0, 1)])
-def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet):
+KEYS = ("trace.refill", "trace.sort", "trace.packet", "trace.spec")
+
+
+@pytest.mark.parametrize("refill,sort,packet,spec", [
+    (1, 0, 0, 0), (4, 0, 0, 0), (16, 0, 0, 0), (32, 1, 0, 0), (4, 1, 0, 0), (32, 1, 1, 0), (32, 0, 1, 0),
+    (32, 0, 0, 1), (32, 1, 0, 1), (32, 1, 1, 1)])
+def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec):
     """Every launch shape of the caster (refill threshold, Morton order,
-    packet traversal of coherent warps) returns the same results in input
-    order, bit for bit: the visiting order differs between shapes, and equal-t
-    candidates are resolved by leaf index, not by the order met."""
+    packet traversal of coherent warps, postponed leaves) returns the same
+    results in input order, bit for bit: the visiting order differs between
+    shapes, and equal-t candidates are resolved by leaf index, not by the
+    order met."""
     tris, sc = mesh_scene(rt, ctx, 6, 7)
     try:
         cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 256, 200)
         rays = np.concatenate([rt.gen_camera_rays(cam, 256, 200), rt.gen_random_rays(11, 40000)])
-        old = (ctx.get_tuning("trace.refill"), ctx.get_tuning("trace.sort"), ctx.get_tuning("trace.packet"))
-        ctx.set_tuning("trace.packet", 0)
+        old = [ctx.get_tuning(k) for k in KEYS]
+        for k, v in zip(KEYS, (32, 0, 0, 0)):
+            ctx.set_tuning(k, v)
         base = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
-        ctx.set_tuning("trace.refill", refill)
-        ctx.set_tuning("trace.sort", sort)
-        ctx.set_tuning("trace.packet", packet)
+        for k, v in zip(KEYS, (refill, sort, packet, spec)):
+            ctx.set_tuning(k, v)
         try:
             got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
             host = sc.trace_host(rays)
             dev_default = gpu_trace(ctx, sc, rays)
         finally:
-            ctx.set_tuning("trace.refill", old[0])
-            ctx.set_tuning("trace.sort", old[1])
-            ctx.set_tuning("trace.packet", old[2])
+            for k, v in zip(KEYS, old):
+                ctx.set_tuning(k, v)
         assert np.array_equal(host.view(np.uint32), dev_default.view(np.uint32))
         assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
     finally:
+        sc.release()
+
+
+def test_single_triangle_scene(rt, orc, ctx):
+    """A one-triangle scene: the root itself is a leaf, in every traversal."""
+    t, m, _ = rt.gen_cornell(1, 0)
+    t = t[:1].copy()
+    sc = ctx.upload_scene(t, m)
+    old = [ctx.get_tuning(k) for k in KEYS]
+    try:
+        cam = rt.camera_look_at([0, 0, -14], [0, -4, 0], [0, 1, 0], 60.0, 64, 64)
+        rays = rt.gen_camera_rays(cam, 64, 64)
+        want = orc.trace(t, sc.bvh(), rays)
+        for spec in (0, 1):
+            ctx.set_tuning("trace.spec", spec)
+            got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+            np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+    finally:
+        for k, v in zip(KEYS, old):
+            ctx.set_tuning(k, v)
         sc.release()
 
 

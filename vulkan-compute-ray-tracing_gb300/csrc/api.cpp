@@ -587,18 +587,19 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
     return RT_SUCCESS;
   }
   const bool refine = (flags & RT_HIT_FP32) == 0;
-  if (opts.sort && n >= 65536) {
-    // Stream-ordered scratch from the device memory pool.
-    void *scratch = nullptr;
-    CK(cudaMallocAsync(&scratch, raysort_scratch_bytes(n), st), "ray sort scratch");
-    uint32_t *perm = nullptr;
-    cudaError_t e = launch_raysort(rays, n, nullptr, scratch, &perm, st);
-    if (e == cudaSuccess) e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st, perm);
-    cudaFreeAsync(scratch, st);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
-    return RT_SUCCESS;
-  }
-  cudaError_t e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st);
+  const bool use_sort = opts.sort && n >= 65536;
+  // Stream-ordered scratch from the device memory pool: the chunk list of
+  // the packet pass, then the ray sort's buffers.
+  const size_t chunk_bytes = (trace_chunk_scratch_bytes(n) + 255) & ~size_t(255);
+  char *scratch = nullptr;
+  CK(cudaMallocAsync((void **)&scratch, chunk_bytes + (use_sort ? raysort_scratch_bytes(n) : 0), st),
+     "trace scratch");
+  uint32_t *perm = nullptr;
+  cudaError_t e = use_sort ? launch_raysort(rays, n, nullptr, scratch + chunk_bytes, &perm, st) : cudaSuccess;
+  if (e == cudaSuccess)
+    e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st, perm,
+                     reinterpret_cast<uint32_t *>(scratch));
+  cudaFreeAsync(scratch, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
   return RT_SUCCESS;
 }
@@ -623,7 +624,8 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
   // the traversal of the other.
   const uint32_t chunk = 1u << 20;
   const size_t io_bytes = (size_t)chunk * (sizeof(rt_ray) + sizeof(rt_hit));
-  const size_t need = io_bytes + raysort_scratch_bytes(chunk);
+  const size_t chunk_bytes = (trace_chunk_scratch_bytes(chunk) + 255) & ~size_t(255);
+  const size_t need = io_bytes + chunk_bytes + raysort_scratch_bytes(chunk);
   if (ctx->stage_bytes < need) {
     for (int i = 0; i < 2; i++) {
       if (ctx->stage[i]) cudaFree(ctx->stage[i]);
@@ -640,9 +642,10 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
     CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
     uint32_t *perm = nullptr;
+    uint32_t *chunks = (uint32_t *)((char *)ctx->stage[s] + io_bytes);
     if (opts.sort && m >= 65536)
-      CK(launch_raysort(dr, m, nullptr, (char *)ctx->stage[s] + io_bytes, &perm, st), "ray sort");
-    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm), "trace launch");
+      CK(launch_raysort(dr, m, nullptr, (char *)ctx->stage[s] + io_bytes + chunk_bytes, &perm, st), "ray sort");
+    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm, chunks), "trace launch");
     CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
   }
   CK(cudaStreamSynchronize(ctx->aux[0]), "trace");
@@ -724,9 +727,24 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.packet = (int)value;
     return RT_SUCCESS;
   }
-  if (k == "trace.smem") {
+  if (k == "trace.spec") {
     if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
-    ctx->trace_opts.smem = (int)value;
+    ctx->trace_opts.spec = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.minblocks") {
+    if (value != 16 && value != 12 && value != 10) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.minblocks = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.packet_minblocks") {
+    if (value != 16 && value != 12 && value != 10) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.packet_minblocks = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.defer") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.defer = (int)value;
     return RT_SUCCESS;
   }
   if (k == "render.mode") {
@@ -759,8 +777,20 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
     *value = ctx->trace_opts.packet;
     return RT_SUCCESS;
   }
-  if (k == "trace.smem") {
-    *value = ctx->trace_opts.smem;
+  if (k == "trace.spec") {
+    *value = ctx->trace_opts.spec;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.minblocks") {
+    *value = ctx->trace_opts.minblocks;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.packet_minblocks") {
+    *value = ctx->trace_opts.packet_minblocks;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.defer") {
+    *value = ctx->trace_opts.defer;
     return RT_SUCCESS;
   }
   if (k == "render.mode") {

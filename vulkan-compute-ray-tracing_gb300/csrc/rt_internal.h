@@ -61,16 +61,22 @@ struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
   int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
-  int smem = 0;     // 1: per-lane traversal stacks in shared memory instead of local memory
+  int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
+  int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
+  int packet_minblocks = 16;  // the same for the packet caster
+  int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
 };
 
 // `counter` is a device word private to this launch (work distribution);
 // `refine` recomputes t, u, v of the winning triangle in fp64.
 // `perm` (may be NULL) gives the order rays are cast in; hits always land
 // at their ray's input index.
+// chunk_scratch holds trace_chunk_scratch_bytes(n) (the packet pass's list of
+// chunks left for the per-lane pass); without it packets are not used.
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
                          uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st,
-                         const uint32_t *perm = nullptr);
+                         const uint32_t *perm = nullptr, uint32_t *chunk_scratch = nullptr);
+size_t trace_chunk_scratch_bytes(uint32_t n);
 // Morton bucketing of a ray batch (raysort.cu); `scratch` holds
 // raysort_scratch_bytes(n); *perm_out points into it.
 size_t raysort_scratch_bytes(uint32_t n);

@@ -152,16 +152,46 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
 // Whole-warp batches: a warp claims 32 consecutive rays (consecutive in
 // Morton order when the batch was reordered). If they share an origin and
 // point the same way (a camera tile), the warp traverses them as one packet
-// (traverse_packet: every lane busy, ~1.5x the nodes of a single ray);
-// otherwise each lane runs its own ray to completion in a tight loop.
-template <int STACK, bool REFINE, bool SMEM>
-__global__ void __launch_bounds__(kTraceBlock, SMEM ? 8 : 16) k_trace_batch(DevScene sc, const float4 *__restrict__ rays,
-                                                             uint32_t n, int4 *__restrict__ hits,
-                                                             uint32_t *__restrict__ counter, uint32_t *err,
-                                                             const uint32_t *__restrict__ perm, int packet) {
+// (traverse_packet: every lane busy, ~1.5x the nodes of a single ray).
+// Other chunks are listed for k_trace_lanes, which runs each lane's ray with
+// postponed leaves, or (no list) each lane runs its own ray in place.
+__device__ __forceinline__ void load_ray(const float4 *__restrict__ rays, uint32_t i, f3 &o, f3 &d, float &tmin,
+                                         float &tmax) {
+  float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
+  o = mk3(r0.x, r0.y, r0.z);
+  d = mk3(r1.x, r1.y, r1.z);
+  tmin = r0.w;
+  tmax = r1.w;
+}
+
+template <bool REFINE>
+__device__ __forceinline__ void store_hit(const DevScene &sc, int4 *__restrict__ hits, uint32_t i, int k, f3 o, f3 d,
+                                          float closest, float u, float v) {
+  int4 h;
+  if (k >= 0) {
+    int tri = __ldg(sc.leaf_tri + k);
+    if (REFINE) refine_fp64(sc.tris, tri, o, d, closest, u, v);
+    h = make_int4(tri, __float_as_int(closest), __float_as_int(u), __float_as_int(v));
+  } else {
+    h = make_int4(-1, 0, 0, 0);
+  }
+  hits[i] = h;
+}
+
+// First kernel of a whole-warp cast: each warp takes 32 consecutive rays (in
+// the cast order); if they are coherent (warp_is_coherent) the warp traces
+// them as one packet, otherwise it lists the chunk for k_trace_lanes (or,
+// without a list, traces it per lane in place). The postponed-leaf traversal
+// lives in the other kernel: compiled into this one it cost the packet path
+// 8% (measured), while the in-place per-lane path costs nothing.
+template <int STACK, bool REFINE, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_packets(DevScene sc, const float4 *__restrict__ rays,
+                                                                   uint32_t n, int4 *__restrict__ hits,
+                                                                   uint32_t *__restrict__ counter, uint32_t *err,
+                                                                   const uint32_t *__restrict__ perm,
+                                                                   uint32_t *__restrict__ list,
+                                                                   uint32_t *__restrict__ list_count) {
   __shared__ int s_stack[kTraceBlock / 32][STACK];
-  // Per-lane traversal stacks in shared memory, one column per thread.
-  __shared__ int s_lane[SMEM ? STACK * kTraceBlock : 1];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     uint32_t base = 0;
@@ -174,32 +204,57 @@ __global__ void __launch_bounds__(kTraceBlock, SMEM ? 8 : 16) k_trace_batch(DevS
     float tmin = 0.0f, tmax = 0.0f;
     if (active) {
       if (perm) i = __ldg(perm + i);
-      float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
-      o = mk3(r0.x, r0.y, r0.z);
-      d = mk3(r1.x, r1.y, r1.z);
-      tmin = r0.w;
-      tmax = r1.w;
+      load_ray(rays, i, o, d, tmin, tmax);
     }
     TraceRay r = make_ray(o, d, tmin);
     float closest = tmax, u = 0.0f, v = 0.0f;
     int k;
-    if (packet && warp_is_coherent(active, r))
+    if (warp_is_coherent(active, r)) {
       k = traverse_packet<STACK>(sc, r, active, closest, u, v, s_stack[warp], err);
-    else if (SMEM)
-      k = active ? traverse_closest_on<STACK>(sc, r, closest, u, v, err, s_lane + threadIdx.x, kTraceBlock) : -1;
+    } else if (list) {
+      if (lane == 0) list[atomicAdd(list_count, 1u)] = base;
+      continue;
+    } else {
+      k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
+    }
+    if (active) store_hit<REFINE>(sc, hits, i, k, o, d, closest, u, v);
+  }
+}
+
+// Per-lane cast of whole-warp chunks: the chunks k_trace_packets listed
+// (list != nullptr) or every chunk of the batch. `spec` selects the
+// postponed-leaf traversal (traverse_spec); results are identical.
+template <int STACK, bool REFINE, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_lanes(DevScene sc, const float4 *__restrict__ rays,
+                                                                   uint32_t n, int4 *__restrict__ hits,
+                                                                   uint32_t *__restrict__ counter, uint32_t *err,
+                                                                   const uint32_t *__restrict__ perm,
+                                                                   const uint32_t *__restrict__ list,
+                                                                   const uint32_t *__restrict__ list_count, int spec) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t chunks = list ? min(*list_count, (n + 31) / 32) : (n + 31) / 32;
+  for (;;) {
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(counter, 1u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= chunks) return;
+    const uint32_t base = list ? __ldg(list + c) : c * 32u;
+    uint32_t i = base + lane;
+    const bool active = i < n;
+    f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
+    float tmin = 0.0f, tmax = 0.0f;
+    if (active) {
+      if (perm) i = __ldg(perm + i);
+      load_ray(rays, i, o, d, tmin, tmax);
+    }
+    TraceRay r = make_ray(o, d, tmin);
+    float closest = tmax, u = 0.0f, v = 0.0f;
+    int k;
+    if (spec)
+      k = traverse_spec<STACK>(sc, r, active, closest, u, v, err);
     else
       k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
-    if (active) {
-      int4 h;
-      if (k >= 0) {
-        int tri = __ldg(sc.leaf_tri + k);
-        if (REFINE) refine_fp64(sc.tris, tri, o, d, closest, u, v);
-        h = make_int4(tri, __float_as_int(closest), __float_as_int(u), __float_as_int(v));
-      } else {
-        h = make_int4(-1, 0, 0, 0);
-      }
-      hits[i] = h;
-    }
+    if (active) store_hit<REFINE>(sc, hits, i, k, o, d, closest, u, v);
   }
 }
 
@@ -217,40 +272,67 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_literal16(DevScene sc, co
 
 int g_num_sms = 0;
 
-template <int STACK, bool REFINE>
-cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                           uint32_t *err, const TraceOpts &opts, const uint32_t *perm, cudaStream_t st) {
-  const bool batch = opts.refill >= 32;
+template <typename K>
+uint32_t persistent_grid(K kernel, uint32_t n) {
   int blocks_per_sm = 0;
-  if (batch && opts.smem)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_batch<STACK, REFINE, true>, kTraceBlock, 0);
-  else if (batch)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_batch<STACK, REFINE, false>, kTraceBlock, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<STACK, REFINE>, kTraceBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kernel, kTraceBlock, 0);
   if (blocks_per_sm < 1) blocks_per_sm = 1;
   uint32_t want = (n + kTraceBlock - 1) / kTraceBlock;
   uint32_t grid = (uint32_t)(g_num_sms * blocks_per_sm);
-  if (grid > want) grid = want;
-  if (batch && opts.smem)
-    k_trace_batch<STACK, REFINE, true><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                                     reinterpret_cast<int4 *>(hits), counter, err,
-                                                                     perm, opts.packet);
-  else if (batch)
-    k_trace_batch<STACK, REFINE, false><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                                      reinterpret_cast<int4 *>(hits), counter, err,
-                                                                      perm, opts.packet);
-  else
-    k_trace<STACK, REFINE><<<grid, kTraceBlock, 0, st>>>(sc, reinterpret_cast<const float4 *>(rays), n,
-                                                         reinterpret_cast<int4 *>(hits), counter, err, opts.refill,
-                                                         perm);
+  return grid > want ? want : grid;
+}
+
+template <int STACK, bool REFINE, int MINB>
+cudaError_t launch_lanes(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
+                         uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
+                         int spec, cudaStream_t st) {
+  auto kern = k_trace_lanes<STACK, REFINE, MINB>;
+  kern<<<persistent_grid(kern, n), kTraceBlock, 0, st>>>(sc, rays, n, hits, counter, err, perm, list, list_count,
+                                                          spec);
+  return cudaGetLastError();
+}
+
+template <int STACK, bool REFINE>
+cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
+                           uint32_t *err, const TraceOpts &opts, const uint32_t *perm, uint32_t *chunk_scratch,
+                           cudaStream_t st) {
+  const float4 *r4 = reinterpret_cast<const float4 *>(rays);
+  int4 *h4 = reinterpret_cast<int4 *>(hits);
+  if (opts.refill >= 32) {
+    // chunk_scratch: [0] listed chunks, [1] lane-pass counter, list from word 64.
+    const uint32_t *list = nullptr, *list_count = nullptr;
+    uint32_t *lane_counter = counter;
+    if (opts.packet && chunk_scratch) {
+      cudaError_t e = cudaMemsetAsync(chunk_scratch, 0, 256, st);
+      if (e != cudaSuccess) return e;
+      auto pk = opts.packet_minblocks >= 16   ? k_trace_packets<STACK, REFINE, 16>
+                : opts.packet_minblocks >= 12 ? k_trace_packets<STACK, REFINE, 12>
+                                              : k_trace_packets<STACK, REFINE, 10>;
+      pk<<<persistent_grid(pk, n), kTraceBlock, 0, st>>>(sc, r4, n, h4, counter, err, perm,
+                                                         opts.defer ? chunk_scratch + 64 : nullptr, chunk_scratch);
+      if (!opts.defer) return cudaGetLastError();
+      list = chunk_scratch + 64;
+      list_count = chunk_scratch;
+      lane_counter = chunk_scratch + 1;
+    }
+    if (opts.minblocks >= 16)
+      return launch_lanes<STACK, REFINE, 16>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec, st);
+    if (opts.minblocks >= 12)
+      return launch_lanes<STACK, REFINE, 12>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec, st);
+    return launch_lanes<STACK, REFINE, 10>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec, st);
+  }
+  auto kt = k_trace<STACK, REFINE>;
+  kt<<<persistent_grid(kt, n), kTraceBlock, 0, st>>>(sc, r4, n, h4, counter, err, opts.refill, perm);
   return cudaGetLastError();
 }
 
 }  // namespace
 
+size_t trace_chunk_scratch_bytes(uint32_t n) { return 4ull * (64 + (n + 31) / 32); }
+
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
-                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st, const uint32_t *perm) {
+                         uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st, const uint32_t *perm,
+                         uint32_t *chunk_scratch) {
   if (n == 0) return cudaSuccess;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -261,10 +343,10 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (sc.depth <= 32)
-    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, opts, perm, st)
-                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, opts, perm, st);
-  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, opts, perm, st)
-                : launch_variant<64, false>(sc, rays, n, hits, counter, err, opts, perm, st);
+    return refine ? launch_variant<32, true>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st)
+                  : launch_variant<32, false>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st);
+  return refine ? launch_variant<64, true>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st)
+                : launch_variant<64, false>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st);
 }
 
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,

@@ -156,6 +156,81 @@ __device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceR
   return traverse_closest_on<STACK>(sc, r, closest, bu, bv, err, stack, 1);
 }
 
+// Per-lane traversal with postponed leaves (Aila and Laine, "Understanding
+// the Efficiency of Ray Traversal on GPUs", HPG 2009, speculative
+// traversal): a lane that reaches a leaf parks it and keeps descending inner
+// nodes until every lane of the warp in the loop holds a leaf; then all
+// parked leaves are tested together. Lanes no longer idle in the inner loop
+// while others are still descending. The extra nodes a lane may visit before
+// its parked triangle shortens `closest` never change the result: every
+// reached triangle is tested with the same acceptance rule. The warp votes
+// only decide when to switch phases. Refs: inner node >= 0, leaf ~k < 0,
+// kEnd (the stack's bottom entry) when the lane is finished.
+template <int STACK>
+__device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay &r, bool active, float &closest,
+                                             float &bu, float &bv, uint32_t *err) {
+  constexpr int kEnd = 0x7fffffff;
+  int stack[STACK];
+  stack[0] = kEnd;
+  int sp = 1;
+  int best = -1;
+  int node = kEnd, leaf = 0;
+  if (active) {
+    float root = slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1], sc.root_lo[2],
+                            sc.root_hi[2], closest);
+    if (root < __int_as_float(0x7f800000)) node = sc.root_ref;
+  }
+  const float4 *__restrict__ bvh = sc.bvh2;
+  while (node != kEnd || leaf < 0) {
+    // A leaf in hand and none parked (only when the root is a leaf).
+    if (node < 0 && leaf >= 0) {
+      leaf = node;
+      node = stack[--sp];
+    }
+    while (node >= 0 && node != kEnd) {
+      const float4 *N = bvh + 4ll * node;
+      float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
+      float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+      float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+      bool h0 = t0 < __int_as_float(0x7f800000), h1 = t1 < __int_as_float(0x7f800000);
+      if (h0 && h1) {
+        int nearc = r0, farc = r1;
+        if (t1 < t0) {
+          nearc = r1;
+          farc = r0;
+        }
+        if (sp >= STACK) {
+          atomicOr(err, KERR_STACK_OVERFLOW);
+          return best;
+        }
+        stack[sp++] = farc;
+        node = nearc;
+      } else if (h0) {
+        node = r0;
+      } else if (h1) {
+        node = r1;
+      } else {
+        node = stack[--sp];
+      }
+      // Park the first leaf reached and keep going.
+      if (node < 0 && leaf >= 0) {
+        leaf = node;
+        node = stack[--sp];
+      }
+      // Every lane still here holds a parked leaf: test them.
+      if (!__any_sync(__activemask(), leaf >= 0)) break;
+    }
+    // The parked leaf, then any leaves the lane stands on.
+    while (leaf < 0) {
+      test_triangle(sc.tpre, sc.leaf_tri, ~leaf, r, closest, best, bu, bv);
+      leaf = node;
+      if (node < 0) node = stack[--sp];
+    }
+  }
+  return best;
+}
+
 // Warp-wide packet traversal for 32 coherent rays: the warp walks one node
 // sequence with one stack (in shared memory, written by lane 0), descending
 // into a child when ANY active lane's box test passes with that lane's own
