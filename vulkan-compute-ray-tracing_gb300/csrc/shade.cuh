@@ -169,7 +169,7 @@ __device__ __forceinline__ bool closest_hit(const DevScene &sc, const PathState 
     return sphere_pass(sc, ps, o, d, hit, rec);
   }
   TraceRay r = make_ray(o, d, kTmin);
-  int k = traverse_closest<STACK>(sc, r, closest, u, v, err);
+  int k = traverse_spec<STACK>(sc, r, true, closest, u, v, err);
   return resolve_hit(sc, ps, o, d, k, closest, rec);
 }
 

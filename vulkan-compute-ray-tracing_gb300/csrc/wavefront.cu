@@ -73,26 +73,44 @@ __global__ void k_wf_raygen(rt_camera cam, uint32_t W, uint32_t H, uint32_t s, r
   rng[p] = (600u * x + y) * (s + 1u);
 }
 
+// Closest triangle per queued ray. A warp whose 32 rays are coherent (the
+// camera rays of bounce 0 in pixel order, or any bundle sharing an origin)
+// traverses them as one packet; other warps run each lane's ray with
+// postponed leaves. Both return every ray's own closest hit.
 template <int STACK>
-__global__ void __launch_bounds__(kWfBlock) k_wf_extend(DevScene sc, const float4 *__restrict__ rays, uint32_t cap,
-                                                        const uint32_t *count, const uint32_t *__restrict__ perm,
-                                                        int2 *__restrict__ hits, uint32_t *counter, uint32_t *err) {
+__global__ void __launch_bounds__(kWfBlock, 12) k_wf_extend(DevScene sc, const float4 *__restrict__ rays,
+                                                            uint32_t cap, const uint32_t *count,
+                                                            const uint32_t *__restrict__ perm,
+                                                            int2 *__restrict__ hits, uint32_t *counter,
+                                                            uint32_t *err) {
+  __shared__ int s_stack[kWfBlock / 32][STACK];
   const uint32_t n = min(cap, *count);
-  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(counter, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) return;
     uint32_t i = base + lane;
-    if (i < n) {
+    const bool active = i < n;
+    f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
+    float tmin = 0.0f, closest = 0.0f;
+    if (active) {
       if (perm) i = __ldg(perm + i);
       float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
-      TraceRay r = make_ray(mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), r0.w);
-      float closest = r1.w, u = 0.0f, v = 0.0f;
-      int k = traverse_closest<STACK>(sc, r, closest, u, v, err);
-      hits[i] = make_int2(k, __float_as_int(closest));
+      o = mk3(r0.x, r0.y, r0.z);
+      d = mk3(r1.x, r1.y, r1.z);
+      tmin = r0.w;
+      closest = r1.w;
     }
+    TraceRay r = make_ray(o, d, tmin);
+    float u = 0.0f, v = 0.0f;
+    int k;
+    if (warp_is_coherent(active, r))
+      k = traverse_packet<STACK>(sc, r, active, closest, u, v, s_stack[warp], err);
+    else
+      k = traverse_spec<STACK>(sc, r, active, closest, u, v, err);
+    if (active) hits[i] = make_int2(k, __float_as_int(closest));
   }
 }
 
