@@ -63,7 +63,7 @@ struct TraceOpts {
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
   int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
-  int packet_minblocks = 16;  // the same for the packet caster
+  int packet_minblocks = 10;  // the same for the packet caster
   int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
 };
 

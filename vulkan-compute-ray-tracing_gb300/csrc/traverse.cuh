@@ -232,62 +232,77 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
 }
 
 // Warp-wide packet traversal for 32 coherent rays: the warp walks one node
-// sequence with one stack (in shared memory, written by lane 0), descending
-// into a child when ANY active lane's box test passes with that lane's own
-// closest t; every active lane then tests each reached leaf's triangle
-// against its own ray. Each lane's result is exactly its per-ray closest hit
-// (the packet visits a superset of every lane's required nodes); only the
-// number of visited nodes changes. Near/far order follows the majority of
-// the lanes that hit both children. All branches are warp-uniform except the
-// triangle test.
+// sequence with one stack, descending into a child when ANY active lane's
+// box test passes with that lane's own closest t; every active lane then
+// tests each reached leaf's triangle against its own ray. Each lane's result
+// is exactly its per-ray closest hit (the packet visits a superset of every
+// lane's required nodes); only the number of visited nodes changes.
+// Inactive lanes carry closest = -inf, so they miss every box and accept no
+// triangle without extra tests. Near/far order follows the first active
+// lane. The stack is warp-distributed in registers for STACK <= 32 (entry j
+// in lane j, read back with a shuffle), else in shared memory. All branches
+// are warp-uniform except inside the triangle test.
 template <int STACK>
 __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRay &r, bool active, float &closest,
                                                float &bu, float &bv, volatile int *stack, uint32_t *err) {
   const uint32_t lane = threadIdx.x & 31;
   const float INF = __int_as_float(0x7f800000);
+  const float saved = closest;
+  if (!active) closest = -INF;
   int best = -1;
-  float root = active ? slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1], sc.root_lo[2],
-                                   sc.root_hi[2], closest)
-                      : INF;
-  if (!__any_sync(0xffffffffu, root < INF)) return -1;
+  const uint32_t act = __ballot_sync(0xffffffffu, active);
+  const int src = act ? __ffs(act) - 1 : 0;
+  float root = slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1], sc.root_lo[2],
+                          sc.root_hi[2], closest);
+  if (!__any_sync(0xffffffffu, root < INF)) {
+    closest = saved;
+    return -1;
+  }
   int sp = 0;
   int node = sc.root_ref;
+  int reg_stack = 0;  // entry `lane` of the register stack (STACK <= 32)
   const float4 *__restrict__ bvh = sc.bvh2;
   for (;;) {
     if (node >= 0) {
       const float4 *N = bvh + 4ll * node;
       float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
-      float t0 = active ? slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest) : INF;
-      float t1 = active ? slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest) : INF;
-      const bool h0 = t0 < INF, h1 = t1 < INF;
-      const uint32_t m0 = __ballot_sync(0xffffffffu, h0), m1 = __ballot_sync(0xffffffffu, h1);
+      float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+      float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      const uint32_t m0 = __ballot_sync(0xffffffffu, t0 < INF), m1 = __ballot_sync(0xffffffffu, t1 < INF);
       const int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
       if (m0 && m1) {
-        const uint32_t pref0 = __ballot_sync(0xffffffffu, h0 && (!h1 || t0 <= t1));
-        const uint32_t pref1 = __ballot_sync(0xffffffffu, h1 && (!h0 || t1 < t0));
-        const bool first0 = __popc(pref0) >= __popc(pref1);
+        // The first active lane's order; a lane that misses a child ranks it last.
+        const bool first0 = __shfl_sync(0xffffffffu, t0 <= t1, src);
         if (sp >= STACK) {
           if (lane == 0) atomicOr(err, KERR_STACK_OVERFLOW);
-          return best;
+          break;
         }
-        if (lane == 0) stack[sp] = first0 ? r1 : r0;
-        __syncwarp();
+        const int farc = first0 ? r1 : r0;
+        if (STACK <= 32) {
+          if (lane == (uint32_t)sp) reg_stack = farc;
+        } else {
+          if (lane == 0) stack[sp] = farc;
+          __syncwarp();
+        }
         sp++;
         node = first0 ? r0 : r1;
+        continue;
       } else if (m0) {
         node = r0;
+        continue;
       } else if (m1) {
         node = r1;
-      } else {
-        if (sp == 0) return best;
-        node = stack[--sp];
+        continue;
       }
     } else {
-      if (active) test_triangle(sc.tpre, sc.leaf_tri, ~node, r, closest, best, bu, bv);
-      if (sp == 0) return best;
-      node = stack[--sp];
+      test_triangle(sc.tpre, sc.leaf_tri, ~node, r, closest, best, bu, bv);
     }
+    if (sp == 0) break;
+    --sp;
+    node = STACK <= 32 ? __shfl_sync(0xffffffffu, reg_stack, sp) : stack[sp];
   }
+  if (!active) closest = saved;
+  return active ? best : -1;
 }
 
 // True when the warp's 32 rays suit packet traversal: active lanes share one
