@@ -306,7 +306,12 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
 }
 
 // True when the warp's 32 rays suit packet traversal: active lanes share one
-// origin and all directions lie within ~18 degrees of the first active one.
+// origin and all directions lie within ~72 degrees of the first active one.
+// Morton-ordered camera rays are within a fraction of a degree of each other
+// except for the few chunks that straddle a jump of the Z-order curve (two
+// tight clusters up to half the field of view apart); a packet over such a
+// chunk visits at most the two clusters' nodes, far cheaper than leaving it
+// to a per-lane pass at the end of the cast.
 __device__ __forceinline__ bool warp_is_coherent(bool active, const TraceRay &r) {
   const uint32_t act = __ballot_sync(0xffffffffu, active);
   if (act == 0) return false;
@@ -319,7 +324,7 @@ __device__ __forceinline__ bool warp_is_coherent(bool active, const TraceRay &r)
   if (active) {
     float dd = r.d.x * dx + r.d.y * dy + r.d.z * dz;
     float n0 = dx * dx + dy * dy + dz * dz, n1 = r.d.x * r.d.x + r.d.y * r.d.y + r.d.z * r.d.z;
-    ok = r.o.x == ox && r.o.y == oy && r.o.z == oz && dd > 0.95f * sqrtf(n0 * n1);
+    ok = r.o.x == ox && r.o.y == oy && r.o.z == oz && dd > 0.3f * sqrtf(n0 * n1);
   }
   return __all_sync(0xffffffffu, ok);
 }
