@@ -229,11 +229,13 @@ typedef struct rt_render_job {
   float *d_rgba32f;
 } rt_render_job;
 
-/* Renders every job with one persistent launch over the pixel tiles of all
- * jobs; per job the image equals rtRender of that job alone (megakernel
- * arithmetic). The reference renders one scene per dispatch
- * (src/main.cpp:228); this is the batched form. Stream-ordered; the job
- * table is copied to the device inside the call. */
+/* Renders every job; per job the image equals rtRender of that job alone.
+ * Jobs that rtRender would give the wavefront kernels ("render.mode" 1, or 2
+ * and at least 2^20 pixels) run one after another on a side stream, while
+ * one persistent launch covers the pixel tiles of all other jobs; the two
+ * overlap on the GPU. The reference renders one scene per dispatch
+ * (src/main.cpp:228); this is the batched form. Returns when the jobs are
+ * done. */
 rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, void *stream);
 
 /* A resident job table for repeated batched launches. Scenes named by the
@@ -241,8 +243,10 @@ rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs,
 typedef struct rt_batch rt_batch;
 rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, rt_batch **out);
 rt_status rtBatchDestroy(rt_ctx *ctx, rt_batch *batch);
-/* One persistent launch over the batch; performs no host synchronisation
- * and no allocation, so it can be captured in a CUDA graph. */
+/* One launch of the batch (the persistent launch plus the side stream's
+ * wavefront jobs, joined back into `stream`); performs no host
+ * synchronisation and no allocation, so it can be captured in a CUDA graph.
+ * The split between the two paths is fixed when the batch is created. */
 rt_status rtBatchLaunch(rt_ctx *ctx, rt_batch *batch, void *stream);
 /* Adds each job's spp to its sample_index on the device (the next
  * progressive frame); capturable. */

@@ -78,6 +78,47 @@ def test_batch_graph_progressive_frames(rt, ctx):
             sc.release()
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+def test_hybrid_batch_with_wavefront_jobs(rt, ctx, mode):
+    """Jobs that rtRender would render with the wavefront kernels (all of
+    them in render.mode 1; the 1024x1024 one in mode 2) run on a side stream
+    next to the persistent launch; every image equals the job alone, for a
+    direct launch and for three progressive graph replays."""
+    import torch
+    scs = scenes(rt, ctx, SPECS[:3])
+    sizes = [(1024, 1024), (128, 96), (200, 40)]
+    old = ctx.get_tuning("render.mode")
+    ctx.set_tuning("render.mode", mode)
+    try:
+        jobs, accs, want, want3 = [], [], [], []
+        for i, (sc, (W, H)) in enumerate(zip(scs, sizes)):
+            cam = rt.camera_look_at([0.2 * i, 0.1, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
+            acc = torch.zeros((H, W, 4), device="cuda")
+            accs.append(acc)
+            jobs.append(rt.make_job(sc, cam, acc, W, H, 1, 5))
+            want.append(render_alone(ctx, sc, cam, W, H, 1, 5))
+            want3.append(render_alone(ctx, sc, cam, W, H, 3, 5))
+        ctx.render_batch(jobs)
+        ctx.synchronize()
+        for a, w in zip(accs, want):
+            assert np.array_equal(a.cpu().numpy().view(np.uint32), w.view(np.uint32))
+        for a in accs:
+            a.zero_()
+        b = ctx.batch(jobs)
+        try:
+            for _ in range(3):
+                b.launch_graph()
+            ctx.synchronize()
+        finally:
+            b.destroy()
+        for a, w in zip(accs, want3):
+            assert np.array_equal(a.cpu().numpy().view(np.uint32), w.view(np.uint32))
+    finally:
+        ctx.set_tuning("render.mode", old)
+        for sc in scs:
+            sc.release()
+
+
 def test_batch_rejects_bad_jobs(rt, ctx):
     import torch
     t, m, s = rt.gen_cornell(1, 10)

@@ -849,11 +849,23 @@ uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) 
 
 }  // namespace rtgb
 
+// A batch is split by image size the way rtRender chooses its kernels: jobs
+// that rtRender would render with the wavefront kernels (render.mode 1, or
+// 2 and >= 2^20 pixels) run one after another on a side stream through the
+// wavefront path, while one persistent launch covers the tiles of all other
+// jobs on the caller's stream. The two overlap: the small jobs fill the SMs
+// that the wavefront's later, shorter bounces leave idle. Every image equals
+// rtRender of its job alone.
 struct rt_batch {
-  BatchJob *d_jobs = nullptr;
+  BatchJob *d_jobs = nullptr;  // persistent-launch jobs
   uint32_t n = 0, total_tiles = 0, max_depth = 0;
-  uint32_t *counter = nullptr;
-  cudaStream_t capture = nullptr;
+  std::vector<BatchJob> wf;    // wavefront jobs (host copies)
+  BatchJob *d_wf = nullptr;    // their device copies: sample_index advances there
+  void *wf_scratch = nullptr;
+  bool wf_sort = true;
+  uint32_t *counter = nullptr; // [0] tile counter, [64] wavefront work counter
+  cudaStream_t side = nullptr, capture = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -898,6 +910,38 @@ rt_status make_jobs(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n, std::vec
   return RT_SUCCESS;
 }
 
+bool wavefront_job(const RenderOpts &o, const rt_render_params &p) {
+  if (p.flags & RT_COMPAT_STACK16) return false;
+  const uint64_t pixels = (uint64_t)p.width * p.height;
+  return pixels < (1ull << 31) && (o.mode == 1 || (o.mode == 2 && pixels >= (1u << 20)));
+}
+
+cudaError_t batch_enqueue(rt_ctx *ctx, rt_batch *b, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (!b->wf.empty()) {
+    if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return e;
+    for (size_t j = 0; j < b->wf.size() && e == cudaSuccess; j++) {
+      const BatchJob &J = b->wf[j];
+      e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx->d_segments, b->counter + 64, ctx->d_err,
+                                  b->wf_scratch, b->wf_sort, b->side, &b->d_wf[j].p.sample_index);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
+  }
+  if (e == cudaSuccess && b->n)
+    e = launch_render_batch(b->d_jobs, b->n, b->total_tiles, b->max_depth, b->counter, ctx->d_segments, ctx->d_err,
+                            st);
+  if (e == cudaSuccess && !b->wf.empty()) e = cudaStreamWaitEvent(st, b->join, 0);
+  return e;
+}
+
+cudaError_t batch_advance(rt_batch *b, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (b->n) e = launch_batch_advance(b->d_jobs, b->n, st);
+  if (e == cudaSuccess && !b->wf.empty()) e = launch_batch_advance(b->d_wf, (uint32_t)b->wf.size(), st);
+  return e;
+}
+
 }  // namespace
 
 extern "C" {
@@ -909,14 +953,49 @@ rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs,
   uint32_t total = 0, depth = 1;
   rt_status s = make_jobs(ctx, jobs, n_jobs, host, total, depth);
   if (s != RT_SUCCESS) return s;
+  RenderOpts ropts;
+  TraceOpts topts;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ropts = ctx->render_opts;
+    topts = ctx->trace_opts;
+  }
+  // Split, then lay the persistent jobs' tiles out again without the others.
+  std::vector<BatchJob> tiles_jobs;
   rt_batch *b = new rt_batch();
-  b->n = n_jobs;
-  b->total_tiles = total;
-  b->max_depth = depth;
-  cudaError_t e = cudaMalloc((void **)&b->d_jobs, sizeof(BatchJob) * std::max(n_jobs, 1u));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->counter, 256);
-  if (e == cudaSuccess && n_jobs)
-    e = cudaMemcpy(b->d_jobs, host.data(), sizeof(BatchJob) * n_jobs, cudaMemcpyHostToDevice);
+  uint64_t tiles = 0;
+  uint32_t max_wf = 0;
+  b->max_depth = 1;
+  for (const BatchJob &J : host) {
+    if (wavefront_job(ropts, J.p)) {
+      b->wf.push_back(J);
+      max_wf = std::max(max_wf, J.p.width * J.p.height);
+    } else {
+      BatchJob T = J;
+      T.tile_begin = (uint32_t)tiles;
+      tiles += batch_tiles(J.p.width, J.p.height);
+      b->max_depth = std::max(b->max_depth, J.sc.depth);
+      tiles_jobs.push_back(T);
+    }
+  }
+  (void)total;
+  (void)depth;
+  b->n = (uint32_t)tiles_jobs.size();
+  b->total_tiles = (uint32_t)tiles;
+  b->wf_sort = topts.sort != 0;
+  cudaError_t e = cudaMalloc((void **)&b->d_jobs, sizeof(BatchJob) * std::max(b->n, 1u));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->counter, 512);
+  if (e == cudaSuccess && b->n)
+    e = cudaMemcpy(b->d_jobs, tiles_jobs.data(), sizeof(BatchJob) * b->n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !b->wf.empty()) {
+    e = cudaMalloc((void **)&b->d_wf, sizeof(BatchJob) * b->wf.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_wf, b->wf.data(), sizeof(BatchJob) * b->wf.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->wf_scratch, wavefront_scratch_bytes(max_wf));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     rtBatchDestroy(ctx, b);
@@ -932,7 +1011,12 @@ rt_status rtBatchDestroy(rt_ctx *ctx, rt_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   if (b->capture) cudaStreamDestroy(b->capture);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
   if (b->d_jobs) cudaFree(b->d_jobs);
+  if (b->d_wf) cudaFree(b->d_wf);
+  if (b->wf_scratch) cudaFree(b->wf_scratch);
   if (b->counter) cudaFree(b->counter);
   delete b;
   return RT_SUCCESS;
@@ -940,15 +1024,13 @@ rt_status rtBatchDestroy(rt_ctx *ctx, rt_batch *b) {
 
 rt_status rtBatchLaunch(rt_ctx *ctx, rt_batch *b, void *stream) {
   if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
-  CK(launch_render_batch(b->d_jobs, b->n, b->total_tiles, b->max_depth, b->counter, ctx->d_segments, ctx->d_err,
-                         pick_stream(ctx, stream)),
-     "batch launch");
+  CK(batch_enqueue(ctx, b, pick_stream(ctx, stream)), "batch launch");
   return RT_SUCCESS;
 }
 
 rt_status rtBatchAdvance(rt_ctx *ctx, rt_batch *b, void *stream) {
   if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
-  CK(launch_batch_advance(b->d_jobs, b->n, pick_stream(ctx, stream)), "batch advance");
+  CK(batch_advance(b, pick_stream(ctx, stream)), "batch advance");
   return RT_SUCCESS;
 }
 
@@ -956,9 +1038,8 @@ rt_status rtBatchLaunchGraph(rt_ctx *ctx, rt_batch *b, void *stream) {
   if (!ctx || !b) return RT_ERR_INVALID_ARGUMENT;
   if (!b->exec) {
     CK(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "graph capture");
-    cudaError_t e = launch_render_batch(b->d_jobs, b->n, b->total_tiles, b->max_depth, b->counter, ctx->d_segments,
-                                        ctx->d_err, b->capture);
-    if (e == cudaSuccess) e = launch_batch_advance(b->d_jobs, b->n, b->capture);
+    cudaError_t e = batch_enqueue(ctx, b, b->capture);
+    if (e == cudaSuccess) e = batch_advance(b, b->capture);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(b->capture, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -975,27 +1056,13 @@ rt_status rtBatchLaunchGraph(rt_ctx *ctx, rt_batch *b, void *stream) {
 rt_status rtRenderBatch(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs, void *stream) {
   if (!ctx || (n_jobs && !jobs)) return RT_ERR_INVALID_ARGUMENT;
   if (n_jobs == 0) return RT_SUCCESS;
-  std::vector<BatchJob> host;
-  uint32_t total = 0, depth = 1;
-  rt_status s = make_jobs(ctx, jobs, n_jobs, host, total, depth);
+  rt_batch *b = nullptr;
+  rt_status s = rtBatchCreate(ctx, jobs, n_jobs, &b);
   if (s != RT_SUCCESS) return s;
   cudaStream_t st = pick_stream(ctx, stream);
-  // Job table and tile counter from the stream-ordered pool; the table is
-  // staged through pinned memory so the copy is asynchronous.
-  BatchJob *d_jobs = nullptr;
-  uint32_t *counter = nullptr;
-  CK(cudaMallocAsync((void **)&d_jobs, sizeof(BatchJob) * n_jobs + 256, st), "batch table");
-  counter = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(d_jobs) + sizeof(BatchJob) * n_jobs);
-  BatchJob *pinned = nullptr;
-  CK(cudaMallocHost((void **)&pinned, sizeof(BatchJob) * n_jobs), "batch staging");
-  std::memcpy(pinned, host.data(), sizeof(BatchJob) * n_jobs);
-  cudaError_t e = cudaMemcpyAsync(d_jobs, pinned, sizeof(BatchJob) * n_jobs, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = launch_render_batch(d_jobs, n_jobs, total, depth, counter, ctx->d_segments, ctx->d_err, st);
-  cudaFreeAsync(d_jobs, st);
-  // The staging buffer must outlive the copy.
-  cudaStreamSynchronize(st);
-  cudaFreeHost(pinned);
+  cudaError_t e = batch_enqueue(ctx, b, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  rtBatchDestroy(ctx, b);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batch launch");
   return RT_SUCCESS;
 }

@@ -94,11 +94,12 @@ cudaError_t launch_render(const DevScene &sc, const rt_camera &cam, const rt_ren
 
 // Wavefront render (wavefront.cu): same images as launch_render; `scratch`
 // holds wavefront_scratch_bytes(width*height); `counter` is a launch-private
-// device word.
+// device word. With d_sample_index the kernels read the first sample index
+// from the device at run time instead of p.sample_index.
 size_t wavefront_scratch_bytes(uint32_t cap);
 cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
                                     unsigned long long *segments, uint32_t *counter, uint32_t *err, void *scratch,
-                                    bool sort, cudaStream_t st);
+                                    bool sort, cudaStream_t st, const uint32_t *d_sample_index = nullptr);
 
 // Render launch-shape knobs (rtSetTuning "render.mode").
 struct RenderOpts {

@@ -60,8 +60,13 @@ WfBufs carve(void *scratch, uint32_t cap) {
   return b;
 }
 
-__global__ void k_wf_raygen(rt_camera cam, uint32_t W, uint32_t H, uint32_t s, rt_ray *rays, uint32_t *slots,
-                            float4 *color, uint32_t *rng, uint32_t *count) {
+// Sample index of this pass: s, or *d_s + s when the index lives on the
+// device (batched jobs advanced by a captured graph).
+__device__ __forceinline__ uint32_t sample_of(uint32_t s, const uint32_t *d_s) { return d_s ? *d_s + s : s; }
+
+__global__ void k_wf_raygen(rt_camera cam, uint32_t W, uint32_t H, uint32_t s, const uint32_t *d_s, rt_ray *rays,
+                            uint32_t *slots, float4 *color, uint32_t *rng, uint32_t *count) {
+  s = sample_of(s, d_s);
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p == 0) *count = W * H;
   if (p >= W * H) return;
@@ -162,8 +167,9 @@ __global__ void __launch_bounds__(kWfBlock) k_wf_shade(DevScene sc, uint32_t fla
   }
 }
 
-__global__ void k_wf_accumulate(uint32_t W, uint32_t H, uint32_t s, uint32_t flags, const float4 *__restrict__ color,
-                                float4 *accum) {
+__global__ void k_wf_accumulate(uint32_t W, uint32_t H, uint32_t s, const uint32_t *d_s, uint32_t flags,
+                                const float4 *__restrict__ color, float4 *accum) {
+  s = sample_of(s, d_s);
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= W * H) return;
   float4 c = color[p];
@@ -195,7 +201,7 @@ size_t wavefront_scratch_bytes(uint32_t cap) {
 
 cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
                                     unsigned long long *segments, uint32_t *counter, uint32_t *err, void *scratch,
-                                    bool sort, cudaStream_t st) {
+                                    bool sort, cudaStream_t st, const uint32_t *d_sample_index) {
   const uint32_t W = p.width, H = p.height, cap = W * H;
   if (cap == 0 || p.spp == 0) return cudaSuccess;
   if (g_sms == 0) {
@@ -214,8 +220,9 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
   if (egrid > grid) egrid = grid;
   cudaError_t e = cudaSuccess;
   for (uint32_t k = 0; k < p.spp; k++) {
-    const uint32_t s = p.sample_index + k;
-    k_wf_raygen<<<grid, kWfBlock, 0, st>>>(cam, W, H, s, b.rays[0], b.slots[0], b.color, b.rng, b.counts);
+    const uint32_t s = d_sample_index ? k : p.sample_index + k;
+    k_wf_raygen<<<grid, kWfBlock, 0, st>>>(cam, W, H, s, d_sample_index, b.rays[0], b.slots[0], b.color, b.rng,
+                                           b.counts);
     for (uint32_t bounce = 0; bounce < p.max_bounces; bounce++) {
       const int in = bounce & 1, out = in ^ 1;
       if ((e = cudaMemsetAsync(b.counts + out, 0, 4, st)) != cudaSuccess) return e;
@@ -231,7 +238,8 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
                                             b.rng, b.rays[out], b.slots[out], b.counts + out,
                                             bounce + 1 == p.max_bounces, segments);
     }
-    k_wf_accumulate<<<grid, kWfBlock, 0, st>>>(W, H, s, p.flags, b.color, reinterpret_cast<float4 *>(accum));
+    k_wf_accumulate<<<grid, kWfBlock, 0, st>>>(W, H, s, d_sample_index, p.flags, b.color,
+                                               reinterpret_cast<float4 *>(accum));
   }
   return cudaGetLastError();
 }
