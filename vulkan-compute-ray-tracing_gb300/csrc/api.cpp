@@ -861,11 +861,14 @@ struct rt_batch {
   uint32_t n = 0, total_tiles = 0, max_depth = 0;
   std::vector<BatchJob> wf;    // wavefront jobs (host copies)
   BatchJob *d_wf = nullptr;    // their device copies: sample_index advances there
-  void *wf_scratch = nullptr;
+  // Wavefront jobs alternate between kSides side streams, each with its own
+  // scratch and work counter (counter[64 * (1 + k)]).
+  static constexpr int kSides = 4;
+  void *wf_scratch[kSides] = {};
   bool wf_sort = true;
-  uint32_t *counter = nullptr; // [0] tile counter, [64] wavefront work counter
-  cudaStream_t side = nullptr, capture = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  uint32_t *counter = nullptr; // [0] tile counter
+  cudaStream_t side[kSides] = {}, capture = nullptr;
+  cudaEvent_t fork = nullptr, join[kSides] = {};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -918,20 +921,23 @@ bool wavefront_job(const RenderOpts &o, const rt_render_params &p) {
 
 cudaError_t batch_enqueue(rt_ctx *ctx, rt_batch *b, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
-  if (!b->wf.empty()) {
+  const int sides = (int)std::min<size_t>(b->wf.size(), rt_batch::kSides);
+  if (sides) {
     if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return e;
+    for (int k = 0; k < sides; k++)
+      if ((e = cudaStreamWaitEvent(b->side[k], b->fork, 0)) != cudaSuccess) return e;
     for (size_t j = 0; j < b->wf.size() && e == cudaSuccess; j++) {
       const BatchJob &J = b->wf[j];
-      e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx->d_segments, b->counter + 64, ctx->d_err,
-                                  b->wf_scratch, b->wf_sort, b->side, &b->d_wf[j].p.sample_index);
+      const int k = (int)(j % rt_batch::kSides);
+      e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx->d_segments, b->counter + 64 * (1 + k), ctx->d_err,
+                                  b->wf_scratch[k], b->wf_sort, b->side[k], &b->d_wf[j].p.sample_index);
     }
-    if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
+    for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaEventRecord(b->join[k], b->side[k]);
   }
   if (e == cudaSuccess && b->n)
     e = launch_render_batch(b->d_jobs, b->n, b->total_tiles, b->max_depth, b->counter, ctx->d_segments, ctx->d_err,
                             st);
-  if (e == cudaSuccess && !b->wf.empty()) e = cudaStreamWaitEvent(st, b->join, 0);
+  for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaStreamWaitEvent(st, b->join[k], 0);
   return e;
 }
 
@@ -984,17 +990,20 @@ rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs,
   b->total_tiles = (uint32_t)tiles;
   b->wf_sort = topts.sort != 0;
   cudaError_t e = cudaMalloc((void **)&b->d_jobs, sizeof(BatchJob) * std::max(b->n, 1u));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->counter, 512);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->counter, 256 * (1 + rt_batch::kSides));
   if (e == cudaSuccess && b->n)
     e = cudaMemcpy(b->d_jobs, tiles_jobs.data(), sizeof(BatchJob) * b->n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !b->wf.empty()) {
     e = cudaMalloc((void **)&b->d_wf, sizeof(BatchJob) * b->wf.size());
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_wf, b->wf.data(), sizeof(BatchJob) * b->wf.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&b->wf_scratch, wavefront_scratch_bytes(max_wf));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    const int sides = (int)std::min<size_t>(b->wf.size(), rt_batch::kSides);
+    for (int k = 0; k < sides && e == cudaSuccess; k++) {
+      e = cudaMalloc(&b->wf_scratch[k], wavefront_scratch_bytes(max_wf));
+      if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
+    }
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -1011,12 +1020,14 @@ rt_status rtBatchDestroy(rt_ctx *ctx, rt_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   if (b->capture) cudaStreamDestroy(b->capture);
-  if (b->side) cudaStreamDestroy(b->side);
+  for (int k = 0; k < rt_batch::kSides; k++) {
+    if (b->side[k]) cudaStreamDestroy(b->side[k]);
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+    if (b->wf_scratch[k]) cudaFree(b->wf_scratch[k]);
+  }
   if (b->fork) cudaEventDestroy(b->fork);
-  if (b->join) cudaEventDestroy(b->join);
   if (b->d_jobs) cudaFree(b->d_jobs);
   if (b->d_wf) cudaFree(b->d_wf);
-  if (b->wf_scratch) cudaFree(b->wf_scratch);
   if (b->counter) cudaFree(b->counter);
   delete b;
   return RT_SUCCESS;
