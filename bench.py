@@ -515,7 +515,7 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--serve-scenes", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=60)
-    ap.add_argument("--serve-rates", default="1,4")
+    ap.add_argument("--serve-rates", default="1,4,64")
     ap.add_argument("--serve-sides", default="256,512,1024")
     ap.add_argument("--serve-spp-max", type=int, default=64)
     ap.add_argument("--serve-active", type=int, default=64)

@@ -843,6 +843,14 @@ unsigned long long *ctx_segments(rt_ctx *ctx) { return ctx->d_segments; }
 uint32_t *ctx_err(rt_ctx *ctx) { return ctx->d_err; }
 uint64_t ctx_budget(rt_ctx *ctx) { return ctx->budget; }
 int ctx_device(rt_ctx *ctx) { return ctx->device; }
+bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort) {
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (sort) *sort = ctx->trace_opts.sort != 0;
+  if (p.flags & RT_COMPAT_STACK16) return false;
+  const uint64_t pixels = (uint64_t)p.width * p.height;
+  const int mode = ctx->render_opts.mode;
+  return pixels < (1ull << 31) && (mode == 1 || (mode == 2 && pixels >= (1u << 20)));
+}
 uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
   return nt ? slab_layout(nt, nm, nl, ns).total : 0;
 }

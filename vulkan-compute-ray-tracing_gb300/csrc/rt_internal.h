@@ -144,6 +144,10 @@ unsigned long long *ctx_segments(rt_ctx *ctx);
 uint32_t *ctx_err(rt_ctx *ctx);
 uint64_t ctx_budget(rt_ctx *ctx);
 int ctx_device(rt_ctx *ctx);
+// True when rtRender would give a render of these params to the wavefront
+// kernels (render.mode 1, or 2 and >= 2^20 pixels; never the 16-entry
+// compat traversal); *sort receives trace.sort.
+bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort);
 // Device bytes rtUploadScene allocates for a scene of these counts.
 uint64_t scene_device_bytes(uint32_t n_triangles, uint32_t n_materials, uint32_t n_lights, uint32_t n_spheres);
 

@@ -5,8 +5,10 @@
 //      scene plus accumulation image fit the budget, evicting resident
 //      scenes that no running request uses, least recently used first;
 //   2. uploads the scenes it admitted requests for (BVH built on the GPU);
-//   3. renders every running request by up to spp_per_step samples in ONE
-//      persistent launch (launch_render_batch over their tiles);
+//   3. renders every running request by up to spp_per_step samples: requests
+//      that rtRender would give the wavefront kernels (large images) run on
+//      side streams, all others in ONE persistent launch over their tiles
+//      (launch_render_batch), the two overlapping on the GPU;
 //   4. retires finished requests (image to the caller's host buffer,
 //      accumulation image freed, latency recorded).
 // Requests that arrive during a step are admitted at the next one, so new
@@ -75,8 +77,14 @@ struct rt_server {
   double busy_since = -1.0;
   cudaStream_t stream = nullptr;
   BatchJob *d_jobs = nullptr, *h_jobs = nullptr;
-  uint32_t *d_counter = nullptr;
+  uint32_t *d_counter = nullptr;  // [0] tile counter, [64 * (1 + k)] side k's work counter
   int device = 0;
+  // Wavefront side streams, their scratch (grown on demand) and join events.
+  static constexpr int kSides = 4;
+  cudaStream_t side[kSides] = {};
+  cudaEvent_t fork = nullptr, join[kSides] = {};
+  void *scratch[kSides] = {};
+  size_t scratch_bytes[kSides] = {};
 };
 
 namespace {
@@ -197,6 +205,8 @@ void scheduler(rt_server *s) {
     uint32_t depth = 1, nj = 0;
     std::vector<uint32_t> step(run.size(), 0);
     std::vector<char> lost(run.size(), 0);
+    std::vector<BatchJob> wf;
+    bool sort = true;
     for (size_t i = 0; i < run.size(); i++) {
       SrvReq *q = run[i];
       SrvScene &sc = s->scenes[q->r.scene];
@@ -207,20 +217,52 @@ void scheduler(rt_server *s) {
       }
       uint32_t left = q->r.spp - q->done_spp;
       step[i] = s->desc.spp_per_step ? std::min(s->desc.spp_per_step, left) : left;
-      BatchJob &B = s->h_jobs[nj++];
+      BatchJob B;
       B.sc = dev;
       B.cam = q->r.camera;
       B.p = rt_render_params{q->r.width, q->r.height, step[i], q->r.max_bounces, q->done_spp, q->r.flags, {0, 0}};
       B.accum = q->d_accum;
+      if (ctx_wavefront_render(s->ctx, B.p, &sort)) {
+        wf.push_back(B);
+        continue;
+      }
       B.tile_begin = (uint32_t)tiles;
       B.tiles_x = batch_tiles_x(q->r.width);
       tiles += batch_tiles(q->r.width, q->r.height);
       depth = std::max(depth, dev.depth);
+      s->h_jobs[nj++] = B;
     }
-    cudaError_t e = cudaMemcpyAsync(s->d_jobs, s->h_jobs, sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess)
+    cudaError_t e = cudaSuccess;
+    const int sides = (int)std::min<size_t>(wf.size(), rt_server::kSides);
+    for (int k = 0; k < sides && e == cudaSuccess; k++) {
+      size_t need = 0;
+      for (size_t j = k; j < wf.size(); j += rt_server::kSides)
+        need = std::max(need, wavefront_scratch_bytes(wf[j].p.width * wf[j].p.height));
+      if (need > s->scratch_bytes[k]) {
+        if (s->scratch[k]) cudaFree(s->scratch[k]);
+        s->scratch[k] = nullptr;
+        s->scratch_bytes[k] = 0;
+        e = cudaMalloc(&s->scratch[k], need);
+        if (e == cudaSuccess) s->scratch_bytes[k] = need;
+      }
+    }
+    if (e == cudaSuccess && sides) {
+      e = cudaEventRecord(s->fork, s->stream);
+      for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaStreamWaitEvent(s->side[k], s->fork, 0);
+      for (size_t j = 0; j < wf.size() && e == cudaSuccess; j++) {
+        const int k = (int)(j % rt_server::kSides);
+        const BatchJob &J = wf[j];
+        e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx_segments(s->ctx), s->d_counter + 64 * (1 + k),
+                                    ctx_err(s->ctx), s->scratch[k], sort, s->side[k]);
+      }
+      for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaEventRecord(s->join[k], s->side[k]);
+    }
+    if (e == cudaSuccess && nj)
+      e = cudaMemcpyAsync(s->d_jobs, s->h_jobs, sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess && nj)
       e = launch_render_batch(s->d_jobs, nj, (uint32_t)tiles, depth, s->d_counter, ctx_segments(s->ctx),
                               ctx_err(s->ctx), s->stream);
+    for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaStreamWaitEvent(s->stream, s->join[k], 0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     // Retire.
     std::vector<SrvReq *> done;
@@ -274,8 +316,19 @@ rt_status rtServerCreate(rt_ctx *ctx, const rt_server_desc *desc, rt_server **ou
   cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_jobs, sizeof(BatchJob) * cap);
   if (e == cudaSuccess) e = cudaMallocHost((void **)&s->h_jobs, sizeof(BatchJob) * cap);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_counter, 256);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_counter, 256 * (1 + rt_server::kSides));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+  for (int k = 0; k < rt_server::kSides && e == cudaSuccess; k++) {
+    e = cudaStreamCreateWithFlags(&s->side[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join[k], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
+    for (int k = 0; k < rt_server::kSides; k++) {
+      if (s->side[k]) cudaStreamDestroy(s->side[k]);
+      if (s->join[k]) cudaEventDestroy(s->join[k]);
+    }
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->d_counter) cudaFree(s->d_counter);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->d_jobs) cudaFree(s->d_jobs);
     if (s->h_jobs) cudaFreeHost(s->h_jobs);
@@ -308,6 +361,13 @@ rt_status rtServerDestroy(rt_server *s) {
     for (SrvScene &c : s->scenes)
       if (c.resident) rtReleaseScene(s->ctx, c.resident);
   }
+  for (int k = 0; k < rt_server::kSides; k++) {
+    if (s->side[k]) cudaStreamSynchronize(s->side[k]);
+    if (s->side[k]) cudaStreamDestroy(s->side[k]);
+    if (s->join[k]) cudaEventDestroy(s->join[k]);
+    if (s->scratch[k]) cudaFree(s->scratch[k]);
+  }
+  if (s->fork) cudaEventDestroy(s->fork);
   cudaStreamDestroy(s->stream);
   cudaFree(s->d_jobs);
   cudaFreeHost(s->h_jobs);
