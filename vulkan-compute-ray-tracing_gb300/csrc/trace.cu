@@ -210,7 +210,10 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_packets(DevScene sc
     float closest = tmax, u = 0.0f, v = 0.0f;
     int k;
     if (warp_is_coherent(active, r)) {
-      k = traverse_packet<STACK>(sc, r, active, closest, u, v, s_stack[warp], err);
+      const int oct = warp_octant(active, r);
+#define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, u, v, s_stack[warp], err)
+      RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
     } else if (list) {
       if (lane == 0) list[atomicAdd(list_count, 1u)] = base;
       continue;
@@ -250,10 +253,14 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_lanes(DevScene sc, 
     TraceRay r = make_ray(o, d, tmin);
     float closest = tmax, u = 0.0f, v = 0.0f;
     int k;
-    if (spec)
-      k = traverse_spec<STACK>(sc, r, active, closest, u, v, err);
-    else
+    if (spec) {
+      const int oct = warp_octant(active, r);
+#define RTGB_CALL(O) k = traverse_spec<STACK, O>(sc, r, active, closest, u, v, err)
+      RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+    } else {
       k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
+    }
     if (active) store_hit<REFINE>(sc, hits, i, k, o, d, closest, u, v);
   }
 }

@@ -58,14 +58,47 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 
 // Slab test of [lo, hi] against [tmin, tmax]; returns the entry distance or
 // +inf when the box is missed.
+//
+// OCT = -1: the near/far plane of each axis is picked with min/max. OCT in
+// 0..7: the caller knows the signs of the ray's inverse direction (bit 0: x
+// negative, bit 1: y, bit 2: z), so the near plane is lo for a positive
+// component and hi for a negative one, chosen at compile time. For boxes with
+// lo <= hi both forms give the same bits: fma(lo, i, -o) <= fma(hi, i, -o)
+// for i > 0 because rounding is monotonic, so min/max pick exactly those
+// values. The fixed form saves six ALU operations per box.
+template <int OCT = -1>
 __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float hx, float ly, float hy, float lz,
                                             float hz, float tmax) {
   float ax = fmaf(lx, r.ix, -r.ox), bx = fmaf(hx, r.ix, -r.ox);
   float ay = fmaf(ly, r.iy, -r.oy), by = fmaf(hy, r.iy, -r.oy);
   float az = fmaf(lz, r.iz, -r.oz), bz = fmaf(hz, r.iz, -r.oz);
-  float tn = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), r.tmin));
-  float tf = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+  float tn, tf;
+  if (OCT < 0) {
+    tn = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), r.tmin));
+    tf = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+  } else {
+    const float nx = (OCT & 1) ? bx : ax, fx = (OCT & 1) ? ax : bx;
+    const float ny = (OCT & 2) ? by : ay, fy = (OCT & 2) ? ay : by;
+    const float nz = (OCT & 4) ? bz : az, fz = (OCT & 4) ? az : bz;
+    tn = max3f(nx, ny, fmaxf(nz, r.tmin));
+    tf = min3f(fx, fy, fminf(fz, tmax));
+  }
   return tn <= tf ? tn : __int_as_float(0x7f800000);
+}
+
+// Sign octant of the ray's inverse direction (the OCT of slab_enter).
+__device__ __forceinline__ int ray_octant(const TraceRay &r) {
+  return (r.ix < 0.0f ? 1 : 0) | (r.iy < 0.0f ? 2 : 0) | (r.iz < 0.0f ? 4 : 0);
+}
+
+// The octant shared by every active lane of the warp, or -1 (mixed, or no
+// active lane). Warp-converged call.
+__device__ __forceinline__ int warp_octant(bool active, const TraceRay &r) {
+  const uint32_t act = __ballot_sync(0xffffffffu, active);
+  if (act == 0) return -1;
+  const int mine = ray_octant(r);
+  const int first = __shfl_sync(0xffffffffu, mine, __ffs(act) - 1);
+  return __all_sync(0xffffffffu, !active || mine == first) ? first : -1;
 }
 
 // triIntersect on a precomputed record; updates (closest, best, u, v) when
@@ -166,7 +199,7 @@ __device__ __forceinline__ int traverse_closest(const DevScene &sc, const TraceR
 // reached triangle is tested with the same acceptance rule. The warp votes
 // only decide when to switch phases. Refs: inner node >= 0, leaf ~k < 0,
 // kEnd (the stack's bottom entry) when the lane is finished.
-template <int STACK>
+template <int STACK, int OCT = -1>
 __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay &r, bool active, float &closest,
                                              float &bu, float &bv, uint32_t *err) {
   constexpr int kEnd = 0x7fffffff;
@@ -190,8 +223,8 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
     while (node >= 0 && node != kEnd) {
       const float4 *N = bvh + 4ll * node;
       float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
-      float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      float t0 = slab_enter<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+      float t1 = slab_enter<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
       int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
       bool h0 = t0 < __int_as_float(0x7f800000), h1 = t1 < __int_as_float(0x7f800000);
       if (h0 && h1) {
@@ -231,6 +264,21 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
   return best;
 }
 
+// Dispatch to the octant-specialised instance when the warp's rays share
+// one sign octant (warp-uniform branch), else the generic one.
+#define RTGB_OCT_DISPATCH(oct, CALL)                     \
+  switch (oct) {                                         \
+    case 0: CALL(0); break;                              \
+    case 1: CALL(1); break;                              \
+    case 2: CALL(2); break;                              \
+    case 3: CALL(3); break;                              \
+    case 4: CALL(4); break;                              \
+    case 5: CALL(5); break;                              \
+    case 6: CALL(6); break;                              \
+    case 7: CALL(7); break;                              \
+    default: CALL(-1); break;                            \
+  }
+
 // Warp-wide packet traversal for 32 coherent rays: the warp walks one node
 // sequence with one stack, descending into a child when ANY active lane's
 // box test passes with that lane's own closest t; every active lane then
@@ -242,7 +290,7 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
 // lane. The stack is warp-distributed in registers for STACK <= 32 (entry j
 // in lane j, read back with a shuffle), else in shared memory. All branches
 // are warp-uniform except inside the triangle test.
-template <int STACK>
+template <int STACK, int OCT = -1>
 __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRay &r, bool active, float &closest,
                                                float &bu, float &bv, volatile int *stack, uint32_t *err) {
   const uint32_t lane = threadIdx.x & 31;
@@ -266,8 +314,8 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
     if (node >= 0) {
       const float4 *N = bvh + 4ll * node;
       float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
-      float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      float t0 = slab_enter<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+      float t1 = slab_enter<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
       const uint32_t m0 = __ballot_sync(0xffffffffu, t0 < INF), m1 = __ballot_sync(0xffffffffu, t1 < INF);
       const int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
       if (m0 && m1) {

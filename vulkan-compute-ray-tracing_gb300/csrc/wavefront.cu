@@ -111,10 +111,16 @@ __global__ void __launch_bounds__(kWfBlock, 12) k_wf_extend(DevScene sc, const f
     TraceRay r = make_ray(o, d, tmin);
     float u = 0.0f, v = 0.0f;
     int k;
-    if (warp_is_coherent(active, r))
-      k = traverse_packet<STACK>(sc, r, active, closest, u, v, s_stack[warp], err);
-    else
-      k = traverse_spec<STACK>(sc, r, active, closest, u, v, err);
+    const int oct = warp_octant(active, r);
+    if (warp_is_coherent(active, r)) {
+#define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, u, v, s_stack[warp], err)
+      RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+    } else {
+#define RTGB_CALL(O) k = traverse_spec<STACK, O>(sc, r, active, closest, u, v, err)
+      RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+    }
     if (active) hits[i] = make_int2(k, __float_as_int(closest));
   }
 }
