@@ -133,6 +133,17 @@ rt_status rtRender(rt_ctx *ctx, rt_scene_id scene, const rt_render_params *param
 rt_status rtExportImage(rt_ctx *ctx, const float *d_rgba32f, uint32_t width, uint32_t height, float gamma,
                         uint8_t *d_rgba8, void *stream);
 
+/* smartDeNoise, the edge-preserving filter the reference's post-process
+ * shader defines (post-process-shader.frag:26-68) and leaves switched off
+ * (frag:73 would blend it 50/50 with the unfiltered image, sigma 2, kSigma 2,
+ * threshold 0.05): out = mix * filtered + (1 - mix) * in, per RGBA32F pixel.
+ * Circular kernel of radius round(kSigma * sigma) <= 64 with fractional row
+ * offsets, spatial Gaussian (sigma) times range Gaussian (threshold) weights,
+ * taps fetched bilinearly with the reference sampler's REPEAT wrap
+ * (src/memory/Image.cpp:353-357). d_in and d_out must not alias. */
+rt_status rtDenoiseImage(rt_ctx *ctx, const float *d_in, uint32_t width, uint32_t height, float sigma,
+                         float ksigma, float threshold, float mix, float *d_out, void *stream);
+
 /* Closest-hit casting for a device batch of rays (the hit_bvh loop of
  * ray-trace-compute.comp:262-311 as a stand-alone query). Stream-ordered. */
 rt_status rtTraceClosest(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,

@@ -35,6 +35,7 @@ def _load():
         "oracle_sort_with_depth": (None, [P, P, U32, I32]),
         "oracle_lights_from_materials": (U32, [P, U32, P, U32, P]),
         "oracle_camera_from_reference": (None, [P, U32, U32, P]),
+        "oracle_denoise": (None, [P, U32, U32, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P]),
         "oracle_trace": (I32, [P, U32, P, U32, P, U32, I32, I32, D, P, P, I32]),
         "oracle_trace_f64": (I32, [P, U32, P, U32, P, U32, P, P, I32]),
         "oracle_render": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
@@ -229,6 +230,15 @@ def render(tris, mats, nodes, lights, spheres, camera: np.ndarray, width: int, h
        len(lights), _p(spheres) if len(spheres) else None, len(spheres), _p(cam), ctypes.addressof(p), _p(accum),
        ctypes.byref(seg), threads)
     return accum, seg.value
+
+
+def denoise(img: np.ndarray, sigma: float = 2.0, ksigma: float = 2.0, threshold: float = 0.05,
+            mix: float = 1.0) -> np.ndarray:
+    """smartDeNoise restatement on an (H, W, 4) float32 image."""
+    img = np.ascontiguousarray(img, np.float32)
+    out = np.zeros_like(img)
+    LIB.oracle_denoise(_p(img), img.shape[1], img.shape[0], sigma, ksigma, threshold, mix, _p(out))
+    return out
 
 
 def max_threads() -> int:

@@ -725,4 +725,53 @@ int oracle_render_f64(const rt_triangle *tris, uint32_t ntris, const rt_material
 }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+// smartDeNoise (post-process-shader.frag:26-68) over an RGBA32F image, as a
+// texel-space restatement: taps at (px + x, py + y) fetched bilinearly with
+// REPEAT wrap (the reference's sampler, src/memory/Image.cpp:353-357), every
+// step one fp32 operation in shader order; out = mix * filtered + (1 - mix)
+// * in. Built with -ffp-contract=off, so no step is fused.
+void oracle_denoise(const float *in, uint32_t W, uint32_t H, float sigma, float ksigma, float threshold, float mix,
+                    float *out) {
+  const float kInvPi = 0.31830988618379067154f, kInvSqrt2Pi = 0.39894228040143267794f;
+  const float radius = std::round(ksigma * sigma), rad_q = radius * radius;
+  const float inv_sigma_q2 = 0.5f / (sigma * sigma), inv_sigma_q2pi = kInvPi * inv_sigma_q2;
+  const float inv_thr_q2 = 0.5f / (threshold * threshold), inv_thr_sqrt2pi = kInvSqrt2Pi / threshold;
+  auto tex = [&](long x, long y, int c) {
+    x %= (long)W;
+    y %= (long)H;
+    if (x < 0) x += W;
+    if (y < 0) y += H;
+    return in[4 * ((size_t)y * W + x) + c];
+  };
+  auto lerp = [](float a, float b, float w) { return (1.0f - w) * a + w * b; };
+#pragma omp parallel for schedule(dynamic, 4)
+  for (long py = 0; py < (long)H; py++) {
+    for (long px = 0; px < (long)W; px++) {
+      float c[4], a[4] = {0, 0, 0, 0}, z = 0.0f;
+      for (int k = 0; k < 4; k++) c[k] = in[4 * ((size_t)py * W + px) + k];
+      for (float x = -radius; x <= radius; x = x + 1.0f) {
+        const float pt = std::sqrt(rad_q - x * x);
+        for (float y = -pt; y <= pt; y = y + 1.0f) {
+          const float dd = x * x + y * y;
+          const float blur = std::exp(-dd * inv_sigma_q2) * inv_sigma_q2pi;
+          const float s = (float)px + x, t = (float)py + y;
+          const float fs = std::floor(s), ft = std::floor(t);
+          const float al = s - fs, be = t - ft;
+          const long i0 = (long)fs, j0 = (long)ft;
+          float w[4];
+          for (int k = 0; k < 4; k++)
+            w[k] = lerp(lerp(tex(i0, j0, k), tex(i0 + 1, j0, k), al), lerp(tex(i0, j0 + 1, k), tex(i0 + 1, j0 + 1, k), al),
+                        be);
+          const float d0 = w[0] - c[0], d1 = w[1] - c[1], d2 = w[2] - c[2], d3 = w[3] - c[3];
+          const float dc2 = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+          const float delta = std::exp(-dc2 * inv_thr_q2) * inv_thr_sqrt2pi * blur;
+          z = z + delta;
+          for (int k = 0; k < 4; k++) a[k] = a[k] + delta * w[k];
+        }
+      }
+      for (int k = 0; k < 4; k++) out[4 * ((size_t)py * W + px) + k] = lerp(c[k], a[k] / z, mix);
+    }
+  }
+}
 }

@@ -186,3 +186,45 @@ def test_export_gamma_rgba8(rt, ctx, tmp_path):
     assert (got[..., 3] == 255).all()
     rt.write_ppm(str(tmp_path / "x.ppm"), d_out.cpu().numpy())
     assert (tmp_path / "x.ppm").stat().st_size == 37 * 53 * 3 + len(b"P6\n53 37\n255\n")
+
+
+@pytest.mark.parametrize("sigma,ksigma,threshold,mix", [(2.0, 2.0, 0.05, 0.5), (1.5, 3.0, 0.2, 1.0),
+                                                        (2.0, 0.0, 0.05, 1.0), (0.7, 2.0, 1.0, 1.0)])
+def test_denoise_matches_oracle(rt, orc, ctx, sigma, ksigma, threshold, mix):
+    """smartDeNoise (post-process-shader.frag:26-68) on a noisy 1-spp render,
+    and on a 7x5 image where the radius-4 kernel wraps around every edge
+    (REPEAT sampler). Tolerance: libm's and CUDA's expf differ in the last
+    ulp, so each weight may differ by ~1e-7 relative."""
+    import torch
+    t, m, s, sc = cornell(rt, ctx, n_soup=2000, n_spheres=3)
+    try:
+        cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 64, 48)
+        img = gpu_render(sc, cam, 64, 48, spp=1, max_bounces=8)
+    finally:
+        sc.release()
+    small = np.random.default_rng(9).uniform(0, 1, (5, 7, 4)).astype(np.float32)
+    for src in (img, small):
+        H, W = src.shape[:2]
+        d_in = torch.from_numpy(np.ascontiguousarray(src)).cuda()
+        d_out = torch.zeros_like(d_in)
+        rt.denoise_image(ctx, d_in, W, H, d_out, sigma, ksigma, threshold, mix)
+        ctx.synchronize()
+        got = d_out.cpu().numpy()
+        want = orc.denoise(src, sigma, ksigma, threshold, mix)
+        assert np.isfinite(want).all()
+        err = np.abs(got.astype(np.float64) - want) / (1.0 + np.abs(want))
+        assert err.max() <= 2e-5, err.max()
+        if ksigma == 0.0:  # radius 0: the centre tap alone, (w * delta) / delta
+            np.testing.assert_allclose(got, src, rtol=1e-6, atol=0)
+
+
+def test_denoise_rejects_bad_arguments(rt, ctx):
+    import torch
+    a = torch.zeros((8, 8, 4), device="cuda")
+    b = torch.zeros_like(a)
+    for args in ((0.0, 2.0, 0.05, 1.0), (2.0, -1.0, 0.05, 1.0), (2.0, 2.0, 0.0, 1.0), (2.0, 2.0, 0.05, 1.5),
+                 (10.0, 10.0, 0.05, 1.0)):
+        with pytest.raises(rt.RtError):
+            rt.denoise_image(ctx, a, 8, 8, b, *args)
+    with pytest.raises(rt.RtError):
+        rt.denoise_image(ctx, a, 8, 8, a)

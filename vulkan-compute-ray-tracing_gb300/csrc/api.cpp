@@ -814,6 +814,19 @@ rt_status rtExportImage(rt_ctx *ctx, const float *d_rgba32f, uint32_t width, uin
   return RT_SUCCESS;
 }
 
+rt_status rtDenoiseImage(rt_ctx *ctx, const float *d_in, uint32_t width, uint32_t height, float sigma,
+                         float ksigma, float threshold, float mix, float *d_out, void *stream) {
+  if (!ctx || !d_in || !d_out || d_in == d_out || (uintptr_t)d_in % 16 || (uintptr_t)d_out % 16)
+    return RT_ERR_INVALID_ARGUMENT;
+  if (!(sigma > 0.0f) || !(ksigma >= 0.0f) || !(threshold > 0.0f) || !(mix >= 0.0f && mix <= 1.0f))
+    return fail(ctx, RT_ERR_INVALID_ARGUMENT, "denoise: sigma > 0, kSigma >= 0, threshold > 0, mix in [0,1]");
+  if (std::round(ksigma * sigma) > 64.0f) return fail(ctx, RT_ERR_INVALID_ARGUMENT, "denoise: radius above 64");
+  if (width > 65536 || height > 65536) return RT_ERR_INVALID_ARGUMENT;
+  CK(launch_denoise(d_in, width, height, sigma, ksigma, threshold, mix, d_out, pick_stream(ctx, stream)),
+     "denoise");
+  return RT_SUCCESS;
+}
+
 rt_status rtSynchronize(rt_ctx *ctx, void *stream) {
   if (!ctx) return RT_ERR_INVALID_ARGUMENT;
   CK(cudaStreamSynchronize(pick_stream(ctx, stream)), "synchronize");

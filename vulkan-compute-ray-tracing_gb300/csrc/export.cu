@@ -2,8 +2,8 @@
 // (resources/shaders/source/post-process-shader.frag:62-68) turns the
 // accumulated image into the displayed one with pow(rgb, 1/2.2) and alpha 1;
 // the swapchain then stores 8 bits per channel. Here that is one pass over
-// the RGBA32F image into an RGBA8 device buffer (the smartDeNoise filter the
-// shader defines is disabled there, frag:64, and is not applied here).
+// the RGBA32F image into an RGBA8 device buffer. The smartDeNoise filter the
+// shader defines (disabled there, frag:73) is a separate pass, denoise.cu.
 #include <cuda_runtime.h>
 
 #include "rt_internal.h"

@@ -136,6 +136,9 @@ rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_
 
 // ---------------------------------------------------------------- export.cu
 cudaError_t launch_export(const float *in, uint32_t n, float gamma, uint8_t *out, cudaStream_t st);
+// smartDeNoise over an RGBA32F image (denoise.cu); in and out must not alias.
+cudaError_t launch_denoise(const float *in, uint32_t W, uint32_t H, float sigma, float ksigma, float threshold,
+                           float mix, float *out, cudaStream_t st);
 
 // ---------------------------------------------------------------- api.cpp
 // Context internals for the serving layer (serve.cpp).

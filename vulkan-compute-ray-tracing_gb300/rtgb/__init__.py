@@ -121,6 +121,7 @@ def _load() -> ctypes.CDLL:
         "rtBatchLaunchGraph": (I32, [P, P, P]),
         "rtBuildBvhNoAlloc": (I32, [P, U32, U32, P, P]),
         "rtExportImage": (I32, [P, P, U32, U32, F32, P, P]),
+        "rtDenoiseImage": (I32, [P, P, U32, U32, F32, F32, F32, F32, P, P]),
         "rtgbGenCornell": (U32, [U64, U32, U32, F32, F32, F32, P, P, P]),
         "rtgbGenIcosphere": (U32, [U64, U32, F32, F32, U32, P]),
         "rtgbGenCameraRays": (None, [ctypes.POINTER(Camera), U32, U32, F32, F32, P]),
@@ -431,6 +432,15 @@ def export_image(ctx: "Context", d_rgba32f, width: int, height: int, d_rgba8, ga
     """RGBA32F device image -> gamma-encoded RGBA8 device image (rtExportImage)."""
     ctx.check(LIB.rtExportImage(ctx.handle, _ptr(d_rgba32f), width, height, gamma, _ptr(d_rgba8), stream),
               "rtExportImage")
+
+
+def denoise_image(ctx: "Context", d_in, width: int, height: int, d_out, sigma: float = 2.0, ksigma: float = 2.0,
+                  threshold: float = 0.05, mix: float = 1.0, stream=None):
+    """smartDeNoise of an RGBA32F device image into another (rtDenoiseImage);
+    the reference's disabled setting is sigma 2, kSigma 2, threshold 0.05,
+    mix 0.5."""
+    ctx.check(LIB.rtDenoiseImage(ctx.handle, _ptr(d_in), width, height, sigma, ksigma, threshold, mix, _ptr(d_out),
+                                 stream), "rtDenoiseImage")
 
 
 def write_ppm(path: str, rgba8: np.ndarray) -> None:
