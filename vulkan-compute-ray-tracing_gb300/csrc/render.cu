@@ -1,7 +1,8 @@
 // Megakernel render: one thread per pixel runs the whole bounce loop of
 // ray-trace-compute.comp:main (352-380) for every sample of the call.
 // Threads are laid out as 8 x 4 pixel tiles per warp so camera rays of a warp
-// are coherent. The number of traced segments (camera + secondary rays) is
+// are coherent: a warp traces its camera segment as one packet, once per
+// call (render_pixel). The number of traced segments (camera + secondary rays) is
 // reduced per warp and added to a 64-bit counter for throughput reporting.
 #include <cuda_runtime.h>
 
@@ -24,13 +25,13 @@ template <int STACK>
 __global__ void __launch_bounds__(kTileX *kTileY) k_render(DevScene sc, rt_camera cam, rt_render_params p,
                                                            float4 *accum, unsigned long long *segments,
                                                            uint32_t *err) {
+  __shared__ int s_stack[kTileX * kTileY / 32][STACK];
+  const uint32_t warp = (threadIdx.y * kTileX + threadIdx.x) >> 5;
   uint32_t x = blockIdx.x * kTileX + threadIdx.x;
   uint32_t y = blockIdx.y * kTileY + threadIdx.y;
-  uint32_t seg = 0;
-  if (x < p.width && y < p.height) {
-    PathState ps = path_state(sc, p.flags);
-    seg = render_pixel<STACK>(sc, ps, cam, p, x, y, accum, err);
-  }
+  const bool active = x < p.width && y < p.height;
+  PathState ps = path_state(sc, p.flags);
+  uint32_t seg = render_pixel<STACK>(sc, ps, cam, p, x, y, active, accum, err, s_stack[warp]);
   count_segments(seg, segments);
 }
 
@@ -44,6 +45,8 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_render_batch(const BatchJob 
                                                                  uint32_t total_tiles, uint32_t *counter,
                                                                  unsigned long long *segments, uint32_t *err) {
   __shared__ uint32_t s_tile;
+  __shared__ int s_stack[kTileX * kTileY / 32][STACK];
+  const uint32_t warp = (threadIdx.y * kTileX + threadIdx.x) >> 5;
   const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
   for (;;) {
     if (leader) s_tile = atomicAdd(counter, 1u);
@@ -62,11 +65,10 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_render_batch(const BatchJob 
     const uint32_t local = tile - J.tile_begin;
     const uint32_t x = (local % J.tiles_x) * kTileX + threadIdx.x;
     const uint32_t y = (local / J.tiles_x) * kTileY + threadIdx.y;
-    uint32_t seg = 0;
-    if (x < p.width && y < p.height) {
-      PathState ps = path_state(sc, p.flags);
-      seg = render_pixel<STACK>(sc, ps, J.cam, p, x, y, reinterpret_cast<float4 *>(J.accum), err);
-    }
+    const bool active = x < p.width && y < p.height;
+    PathState ps = path_state(sc, p.flags);
+    uint32_t seg =
+        render_pixel<STACK>(sc, ps, J.cam, p, x, y, active, reinterpret_cast<float4 *>(J.accum), err, s_stack[warp]);
     count_segments(seg, segments);
   }
 }

@@ -261,15 +261,26 @@ __device__ __forceinline__ bool scatter(const DevScene &sc, const PathState &ps,
 
 // ray_color (comp:314-338) for the camera ray through pixel (x, y);
 // `segments` counts traced segments.
+// k0 value that asks ray_color to trace the first segment itself.
+constexpr int kTraceFirst = -2;
+
 template <int STACK>
-__device__ __forceinline__ f3 ray_color(const DevScene &sc, const PathState &ps, f3 o, f3 dir, uint32_t max_bounces,
-                                        Rng &g, uint32_t &segments, uint32_t *err) {
+__device__ __forceinline__ f3 ray_color(const DevScene &sc, const PathState &ps, f3 o, f3 d, int k0, float t0,
+                                        uint32_t max_bounces, Rng &g, uint32_t &segments, uint32_t *err) {
+  // The bounce loop of comp:314-338. The first segment's triangle result
+  // (leaf k0, distance t0) comes from the caller, which traces it once for
+  // every sample; the sphere pass and the hit record are redone here.
   f3 color = mk3(1.0f, 1.0f, 1.0f);
-  f3 d = normalize3(dir);
   for (uint32_t i = 0; i < max_bounces; i++) {
     HitRec rec;
-    segments++;
-    if (closest_hit<STACK>(sc, ps, o, d, rec, err)) {
+    bool hit;
+    if (i == 0 && k0 != kTraceFirst) {
+      hit = resolve_hit(sc, ps, o, d, k0, t0, rec);
+    } else {
+      segments++;
+      hit = closest_hit<STACK>(sc, ps, o, d, rec, err);
+    }
+    if (hit) {
       f3 albedo, nd;
       bool emits = scatter(sc, ps, d, rec, g, albedo, nd);
       color = mulv3(color, albedo);
@@ -282,6 +293,32 @@ __device__ __forceinline__ f3 ray_color(const DevScene &sc, const PathState &ps,
     }
   }
   return color;
+}
+
+// Triangles along the camera segment of a warp's pixels (warp-converged call;
+// inactive lanes take part without a ray): coherent warps traverse as one
+// packet, others lane by lane with postponed leaves. Returns the leaf index
+// (or -1) and its distance in t; kTraceFirst under the 16-entry compat
+// traversal, which stays per sample as in the shader.
+template <int STACK>
+__device__ __forceinline__ int camera_hit(const DevScene &sc, const PathState &ps, f3 o, f3 d, bool active,
+                                          float &t, uint32_t *err, volatile int *s_stack) {
+  if (ps.flags & RT_COMPAT_STACK16) return kTraceFirst;
+  TraceRay r = make_ray(o, d, kTmin);
+  float closest = kTmax, u = 0.0f, v = 0.0f;
+  int k;
+  const int oct = warp_octant(active, r);
+  if (warp_is_coherent(active, r)) {
+#define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, u, v, s_stack, err)
+    RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+  } else {
+#define RTGB_CALL(O) k = traverse_spec<STACK, O>(sc, r, active, closest, u, v, err)
+    RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+  }
+  t = closest;
+  return k;
 }
 
 // Camera ray direction for pixel (x, y) (comp:371-372).
@@ -297,18 +334,31 @@ __device__ __forceinline__ float unorm8(float x) {
 }
 
 // spp samples of one pixel accumulated into the running mean (comp:375-379).
+// Warp-converged call; `active` lanes own a pixel. The camera ray carries no
+// jitter (comp:371-372: uv = gid / size), so every sample of the call starts
+// with the same first segment: its triangles are traversed once (camera_hit)
+// and each sample's bounce loop continues from that result with its own RNG
+// stream, which gives the same image as tracing it per sample. Returns the
+// number of segments traced.
 template <int STACK>
 __device__ __forceinline__ uint32_t render_pixel(const DevScene &sc, const PathState &ps, const rt_camera &cam,
-                                                 const rt_render_params &p, uint32_t x, uint32_t y, float4 *accum,
-                                                 uint32_t *err) {
+                                                 const rt_render_params &p, uint32_t x, uint32_t y, bool active,
+                                                 float4 *accum, uint32_t *err, volatile int *s_stack) {
   f3 org = ld3(cam.origin);
-  f3 dir = camera_dir(cam, x, y, p.width, p.height);
-  float4 acc = accum[(size_t)y * p.width + x];
+  f3 d0 = active ? normalize3(camera_dir(cam, x, y, p.width, p.height)) : mk3(1.0f, 0.0f, 0.0f);
+  int k0 = kTraceFirst;
+  float t0 = 0.0f;
   uint32_t segments = 0;
+  if (p.max_bounces > 0 && p.spp > 0) {  // uniform across the warp (one job per tile)
+    k0 = camera_hit<STACK>(sc, ps, org, d0, active, t0, err, s_stack);
+    if (k0 != kTraceFirst && active) segments = 1;
+  }
+  if (!active) return 0;
+  float4 acc = accum[(size_t)y * p.width + x];
   for (uint32_t k = 0; k < p.spp; k++) {
     uint32_t s = p.sample_index + k;
     Rng g{(600u * x + y) * (s + 1u)};
-    f3 c = ray_color<STACK>(sc, ps, org, dir, p.max_bounces, g, segments, err);
+    f3 c = ray_color<STACK>(sc, ps, org, d0, k0, t0, p.max_bounces, g, segments, err);
     float sf = (float)s;
     float keep = gmin(sf, 1.0f);
     float den = __fadd_rn(sf, 1.0f);

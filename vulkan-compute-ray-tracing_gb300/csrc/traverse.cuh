@@ -293,7 +293,9 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
 template <int STACK, int OCT = -1>
 __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRay &r, bool active, float &closest,
                                                float &bu, float &bv, volatile int *stack, uint32_t *err) {
-  const uint32_t lane = threadIdx.x & 31;
+  // Hardware lane id: callers run 1-D and 2-D blocks alike.
+  uint32_t lane;
+  asm("mov.u32 %0, %%laneid;" : "=r"(lane));
   const float INF = __int_as_float(0x7f800000);
   const float saved = closest;
   if (!active) closest = -INF;
@@ -348,6 +350,11 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
     if (sp == 0) break;
     --sp;
     node = STACK <= 32 ? __shfl_sync(0xffffffffu, reg_stack, sp) : stack[sp];
+    // A popped ref is an inner node (< ntris - 1) or a leaf ~k (k < ntris).
+    if (node >= (int)sc.ntris - 1 || node < -(int)sc.ntris) {
+      if (lane == 0) atomicOr(err, KERR_BAD_INDEX);
+      break;
+    }
   }
   if (!active) closest = saved;
   return active ? best : -1;

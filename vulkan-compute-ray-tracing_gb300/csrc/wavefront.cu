@@ -31,6 +31,7 @@ struct WfBufs {
   rt_ray *rays[2];
   uint32_t *slots[2];
   int2 *hits;
+  int2 *cam_hits;  // bounce-0 hits of the call's first sample, reused by the others
   float4 *color;
   uint32_t *rng;
   uint32_t *counts;  // [0], [1]: queue lengths
@@ -49,6 +50,8 @@ WfBufs carve(void *scratch, uint32_t cap) {
     p += a256(4ull * cap);
   }
   b.hits = reinterpret_cast<int2 *>(p);
+  p += a256(8ull * cap);
+  b.cam_hits = reinterpret_cast<int2 *>(p);
   p += a256(8ull * cap);
   b.color = reinterpret_cast<float4 *>(p);
   p += a256(16ull * cap);
@@ -201,7 +204,7 @@ int g_sms = 0;
 }  // namespace
 
 size_t wavefront_scratch_bytes(uint32_t cap) {
-  return 2 * (a256(sizeof(rt_ray) * (size_t)cap) + a256(4ull * cap)) + a256(8ull * cap) + a256(16ull * cap) +
+  return 2 * (a256(sizeof(rt_ray) * (size_t)cap) + a256(4ull * cap)) + 2 * a256(8ull * cap) + a256(16ull * cap) +
          a256(4ull * cap) + 256 + a256(raysort_scratch_bytes(cap));
 }
 
@@ -232,6 +235,14 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
     for (uint32_t bounce = 0; bounce < p.max_bounces; bounce++) {
       const int in = bounce & 1, out = in ^ 1;
       if ((e = cudaMemsetAsync(b.counts + out, 0, 4, st)) != cudaSuccess) return e;
+      // Camera rays carry no jitter: bounce 0 is the same for every sample
+      // of the call (queue slot = pixel), so later samples reuse its hits.
+      if (bounce == 0 && k > 0) {
+        k_wf_shade<<<grid, kWfBlock, 0, st>>>(sc, p.flags, b.rays[in], b.slots[in], b.counts + in, b.cam_hits,
+                                              b.color, b.rng, b.rays[out], b.slots[out], b.counts + out,
+                                              bounce + 1 == p.max_bounces, nullptr);
+        continue;
+      }
       uint32_t *perm = nullptr;
       if (sort && (e = launch_raysort(b.rays[in], cap, b.counts + in, b.sort, &perm, st)) != cudaSuccess) return e;
       if ((e = cudaMemsetAsync(counter, 0, 4, st)) != cudaSuccess) return e;
@@ -240,6 +251,9 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
         k_wf_extend<32><<<egrid, kWfBlock, 0, st>>>(sc, r4, cap, b.counts + in, perm, b.hits, counter, err);
       else
         k_wf_extend<64><<<egrid, kWfBlock, 0, st>>>(sc, r4, cap, b.counts + in, perm, b.hits, counter, err);
+      if (bounce == 0 && p.spp > 1 &&
+          (e = cudaMemcpyAsync(b.cam_hits, b.hits, 8ull * cap, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+        return e;
       k_wf_shade<<<grid, kWfBlock, 0, st>>>(sc, p.flags, b.rays[in], b.slots[in], b.counts + in, b.hits, b.color,
                                             b.rng, b.rays[out], b.slots[out], b.counts + out,
                                             bounce + 1 == p.max_bounces, segments);
