@@ -185,8 +185,10 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   traversal (no postponed leaves)
  *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
  *                   1 wavefront (per-bounce kernels over compacted queues),
- *                   2 (default) wavefront from 1024x1024 pixels up; images are
- *                   identical in every mode
+ *                   2 (default) wavefront from render.wavefront_pixels up;
+ *                   images are identical in every mode
+ *   "render.wavefront_pixels"  the mode-2 threshold (default 2^20 pixels);
+ *                   also splits batches and the render server's steps
  *   "bvh.builder"   tree built by rtUploadScene when no nodes are given:
  *                   0 (default) the reference's Bvh.h tree, node-for-node;
  *                   1 a linear BVH over Morton-ordered centroids,
@@ -195,10 +197,28 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   the reference's tree, but closest hits are identical
  *                   (equal-t ties go to the lower triangle index in every
  *                   tree); rtDownloadBvh returns the tree that was built
- * Values persist for the context; the autotuner (rtgb.autotune) writes
+ * Values persist for the context; rtAutotuneTrace / rtAutotuneRender write
  * them. Unknown keys return RT_ERR_INVALID_ARGUMENT. */
 rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);
 rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value);
+
+/* Autotuner (no counterpart in the reference, whose launch shape is fixed at
+ * compile time). Times the closest-hit launch shapes on the caller's own
+ * device rays (coordinate descent over trace.defer, trace.spec,
+ * trace.minblocks, trace.packet_minblocks, trace.sort; `reps` timed casts
+ * per candidate after one warm-up) and keeps the fastest. Hits are identical
+ * in every shape; d_hits receives them. The rates before and after tuning
+ * are returned in Grays/s (either pointer may be NULL). Synchronous. */
+rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, uint32_t n, rt_hit *d_hits,
+                          uint32_t reps, double *start_grays, double *best_grays);
+/* Times megakernel against wavefront renders of the scene (its current
+ * camera; spp samples, max_bounces) at square sizes 256, 512, ... up to
+ * max_side (256..4096) and sets render.wavefront_pixels to the smallest
+ * size from which the wavefront is faster (2^31 when it never is). Images
+ * are identical either way. Synchronous; allocates one image of max_side^2
+ * pixels for the duration of the call. */
+rt_status rtAutotuneRender(rt_ctx *ctx, rt_scene_id scene, uint32_t spp, uint32_t max_bounces, uint32_t max_side,
+                           uint64_t *wavefront_pixels);
 
 /* Waits for the stream (NULL: the context stream) and reports any error a
  * kernel recorded since the last call (e.g. RT_ERR_STACK_OVERFLOW). */

@@ -228,3 +228,18 @@ def test_denoise_rejects_bad_arguments(rt, ctx):
             rt.denoise_image(ctx, a, 8, 8, b, *args)
     with pytest.raises(rt.RtError):
         rt.denoise_image(ctx, a, 8, 8, a)
+
+
+def test_autotune_render_sets_split(rt, ctx):
+    t, m, s, sc = cornell(rt, ctx, n_soup=3000, n_spheres=2)
+    old = (ctx.get_tuning("render.mode"), ctx.get_tuning("render.wavefront_pixels"))
+    try:
+        sc.set_camera(rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 64, 64))
+        px = rt.autotune_render(sc, spp=1, max_bounces=3, max_side=512)
+        assert px in (256 * 256, 512 * 512, 1 << 31)
+        assert ctx.get_tuning("render.wavefront_pixels") == px
+        assert ctx.get_tuning("render.mode") == old[0]
+    finally:
+        ctx.set_tuning("render.mode", old[0])
+        ctx.set_tuning("render.wavefront_pixels", old[1])
+        sc.release()

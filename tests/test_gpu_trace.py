@@ -297,3 +297,28 @@ def test_alt_tree_mode_same_hits(rt, orc, ctx, builder):
     finally:
         sc.release()
         ref_sc.release()
+
+
+def test_autotune_trace_keeps_hits(rt, orc, ctx):
+    """The autotuner's candidates are timing choices only: after tuning, the
+    hits equal the ones cast with the settings it started from."""
+    keys = ("trace.defer", "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort")
+    old = [ctx.get_tuning(k) for k in keys]
+    tris, sc = mesh_scene(rt, ctx, 6, 3)
+    try:
+        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 256, 256)
+        rays = np.concatenate([rt.gen_camera_rays(cam, 256, 256), rt.gen_random_rays(8, 1 << 16)])
+        want = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+        import torch
+        d_rays = dev(rays)
+        d_hits = torch.zeros((len(rays), 4), dtype=torch.float32, device="cuda")
+        before, after = rt.autotune_trace(sc, d_rays, len(rays), d_hits, reps=1)
+        assert before > 0 and after > 0
+        for k in keys:
+            assert ctx.get_tuning(k) in ((16, 12, 10) if "minblocks" in k else (0, 1))
+        got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    finally:
+        for k, v in zip(keys, old):
+            ctx.set_tuning(k, v)
+        sc.release()

@@ -68,3 +68,8 @@ def test_null_arguments_are_rejected(rt):
     p = (ctypes.c_float * 3)(0, 0, 0)
     assert rt.LIB.rtCameraFromReference(p, 0, 8, ctypes.byref(cam)) == 1
     assert rt.LIB.rtCameraLookAt(p, p, p, 40.0, 8, 8, ctypes.byref(cam)) == 1  # eye == target
+
+
+def test_autotuner_rejects_missing_context(rt):
+    assert rt.LIB.rtAutotuneTrace(None, 1, None, 0, None, 1, None, None) == 1
+    assert rt.LIB.rtAutotuneRender(None, 1, 1, 8, 1024, None) == 1

@@ -680,9 +680,7 @@ rt_status rtRender(rt_ctx *ctx, rt_scene_id id, const rt_render_params *p, float
     topts = ctx->trace_opts;
   }
   const uint64_t pixels = (uint64_t)p->width * p->height;
-  bool wavefront = ropts.mode == 1 || (ropts.mode == 2 && pixels >= (1u << 20));
-  if (p->flags & RT_COMPAT_STACK16) wavefront = false;  // the literal 16-entry traversal runs in the megakernel
-  if (wavefront && pixels < (1ull << 31)) {
+  if (use_wavefront(ropts, *p)) {
     void *scratch = nullptr;
     CK(cudaMallocAsync(&scratch, wavefront_scratch_bytes((uint32_t)pixels), st), "wavefront scratch");
     cudaError_t e = launch_render_wavefront(d, cam, *p, accum, ctx->d_segments, next_counter(ctx), ctx->d_err, scratch,
@@ -747,6 +745,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.defer = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "render.wavefront_pixels") {
+    if (value < 1 || value > (1ll << 31)) return RT_ERR_INVALID_ARGUMENT;
+    ctx->render_opts.wavefront_pixels = (uint64_t)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.mode") {
     if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.mode = (int)value;
@@ -795,6 +798,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "render.mode") {
     *value = ctx->render_opts.mode;
+    return RT_SUCCESS;
+  }
+  if (k == "render.wavefront_pixels") {
+    *value = (int64_t)ctx->render_opts.wavefront_pixels;
     return RT_SUCCESS;
   }
   if (k == "bvh.builder") {
@@ -856,13 +863,11 @@ unsigned long long *ctx_segments(rt_ctx *ctx) { return ctx->d_segments; }
 uint32_t *ctx_err(rt_ctx *ctx) { return ctx->d_err; }
 uint64_t ctx_budget(rt_ctx *ctx) { return ctx->budget; }
 int ctx_device(rt_ctx *ctx) { return ctx->device; }
+cudaStream_t ctx_stream(rt_ctx *ctx) { return ctx->stream; }
 bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort) {
   std::lock_guard<std::mutex> g(ctx->mu);
   if (sort) *sort = ctx->trace_opts.sort != 0;
-  if (p.flags & RT_COMPAT_STACK16) return false;
-  const uint64_t pixels = (uint64_t)p.width * p.height;
-  const int mode = ctx->render_opts.mode;
-  return pixels < (1ull << 31) && (mode == 1 || (mode == 2 && pixels >= (1u << 20)));
+  return use_wavefront(ctx->render_opts, p);
 }
 uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
   return nt ? slab_layout(nt, nm, nl, ns).total : 0;
@@ -934,11 +939,7 @@ rt_status make_jobs(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n, std::vec
   return RT_SUCCESS;
 }
 
-bool wavefront_job(const RenderOpts &o, const rt_render_params &p) {
-  if (p.flags & RT_COMPAT_STACK16) return false;
-  const uint64_t pixels = (uint64_t)p.width * p.height;
-  return pixels < (1ull << 31) && (o.mode == 1 || (o.mode == 2 && pixels >= (1u << 20)));
-}
+bool wavefront_job(const RenderOpts &o, const rt_render_params &p) { return use_wavefront(o, p); }
 
 cudaError_t batch_enqueue(rt_ctx *ctx, rt_batch *b, cudaStream_t st) {
   cudaError_t e = cudaSuccess;

@@ -103,8 +103,15 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
 
 // Render launch-shape knobs (rtSetTuning "render.mode").
 struct RenderOpts {
-  int mode = 2;  // 0 megakernel, 1 wavefront, 2 choose by image size
+  int mode = 2;                         // 0 megakernel, 1 wavefront, 2 choose by image size
+  uint64_t wavefront_pixels = 1u << 20;  // mode 2: wavefront from this many pixels up
 };
+// True when a render of these params goes to the wavefront kernels.
+inline bool use_wavefront(const RenderOpts &o, const rt_render_params &p) {
+  if (p.flags & RT_COMPAT_STACK16) return false;  // the literal 16-entry traversal is megakernel-only
+  const uint64_t pixels = (uint64_t)p.width * p.height;
+  return pixels < (1ull << 31) && (o.mode == 1 || (o.mode == 2 && pixels >= o.wavefront_pixels));
+}
 
 // Tree used when a scene is uploaded without nodes (rtSetTuning "bvh.builder").
 struct BuildOpts {
@@ -147,6 +154,7 @@ unsigned long long *ctx_segments(rt_ctx *ctx);
 uint32_t *ctx_err(rt_ctx *ctx);
 uint64_t ctx_budget(rt_ctx *ctx);
 int ctx_device(rt_ctx *ctx);
+cudaStream_t ctx_stream(rt_ctx *ctx);
 // True when rtRender would give a render of these params to the wavefront
 // kernels (render.mode 1, or 2 and >= 2^20 pixels; never the 16-entry
 // compat traversal); *sort receives trace.sort.

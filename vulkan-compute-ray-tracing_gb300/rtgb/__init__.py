@@ -122,6 +122,9 @@ def _load() -> ctypes.CDLL:
         "rtBuildBvhNoAlloc": (I32, [P, U32, U32, P, P]),
         "rtExportImage": (I32, [P, P, U32, U32, F32, P, P]),
         "rtDenoiseImage": (I32, [P, P, U32, U32, F32, F32, F32, F32, P, P]),
+        "rtAutotuneTrace": (I32, [P, U32, P, U32, P, U32, ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(ctypes.c_double)]),
+        "rtAutotuneRender": (I32, [P, U32, U32, U32, U32, ctypes.POINTER(U64)]),
         "rtgbGenCornell": (U32, [U64, U32, U32, F32, F32, F32, P, P, P]),
         "rtgbGenIcosphere": (U32, [U64, U32, F32, F32, U32, P]),
         "rtgbGenCameraRays": (None, [ctypes.POINTER(Camera), U32, U32, F32, F32, P]),
@@ -432,6 +435,24 @@ def export_image(ctx: "Context", d_rgba32f, width: int, height: int, d_rgba8, ga
     """RGBA32F device image -> gamma-encoded RGBA8 device image (rtExportImage)."""
     ctx.check(LIB.rtExportImage(ctx.handle, _ptr(d_rgba32f), width, height, gamma, _ptr(d_rgba8), stream),
               "rtExportImage")
+
+
+def autotune_trace(scene: "Scene", d_rays, n: int, d_hits, reps: int = 3):
+    """Times the closest-hit launch shapes on these device rays and keeps the
+    fastest (rtAutotuneTrace). Returns (Grays/s before, Grays/s after)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    scene.ctx.check(LIB.rtAutotuneTrace(scene.ctx.handle, scene.id, _ptr(d_rays), n, _ptr(d_hits), reps,
+                                        ctypes.byref(a), ctypes.byref(b)), "rtAutotuneTrace")
+    return a.value, b.value
+
+
+def autotune_render(scene: "Scene", spp: int = 1, max_bounces: int = 8, max_side: int = 2048) -> int:
+    """Chooses the megakernel/wavefront split for this scene (rtAutotuneRender);
+    returns the new render.wavefront_pixels."""
+    px = ctypes.c_uint64()
+    scene.ctx.check(LIB.rtAutotuneRender(scene.ctx.handle, scene.id, spp, max_bounces, max_side, ctypes.byref(px)),
+                    "rtAutotuneRender")
+    return px.value
 
 
 def denoise_image(ctx: "Context", d_in, width: int, height: int, d_out, sigma: float = 2.0, ksigma: float = 2.0,
