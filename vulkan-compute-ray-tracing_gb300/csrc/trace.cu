@@ -1,6 +1,10 @@
-// Closest-hit ray casting: one thread per ray, rays fetched by warps from a
-// global work counter (persistent launch sized to the SM count), so warps
-// that finish early pick up new rays instead of idling behind long ones.
+// Closest-hit ray casting. Persistent launches sized to the SM count fetch
+// work from a global counter. The default whole-warp cast runs two kernels
+// per batch: k_trace_packets takes 32 consecutive rays (Morton order) per
+// warp and traverses coherent ones as a packet, listing the rest, and
+// k_trace_lanes casts the listed chunks one ray per lane with postponed
+// leaves. k_trace is the per-lane refill form (a warp claims new rays as
+// lanes finish), k_trace_literal16 the shader's literal traversal.
 //
 // The hit is chosen with the reference's fp32 arithmetic (traverse.cuh).
 // Unless RT_HIT_FP32 is set, t, u, v of the chosen triangle are then
