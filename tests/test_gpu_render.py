@@ -243,3 +243,22 @@ def test_autotune_render_sets_split(rt, ctx):
         ctx.set_tuning("render.mode", old[0])
         ctx.set_tuning("render.wavefront_pixels", old[1])
         sc.release()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_partial_tiles_multi_sample_vs_oracle(rt, orc, ctx, mode):
+    """A 101x37 image (tiles cut on both axes, so warps hold pixels outside
+    the image) with 3 samples per call: the shared camera segment and the
+    per-sample bounces match the oracle, megakernel and wavefront alike."""
+    t, m, s, sc = cornell(rt, ctx, n_soup=4000, n_spheres=3, seed=4)
+    old = ctx.get_tuning("render.mode")
+    try:
+        ctx.set_tuning("render.mode", mode)
+        cam = rt.camera_look_at([0.5, 0.3, -14], [0, 0, 0], [0, 1, 0], 40.0, 101, 37)
+        img = gpu_render(sc, cam, 101, 37, spp=3, max_bounces=8, sample_index=1)
+        want, _ = orc.render(t, m, sc.bvh(), sc.lights(), s, cam.as_array(), 101, 37, spp=3, max_bounces=8,
+                             sample_index=1)
+        assert (mae(img, want) <= TOL).all()
+    finally:
+        ctx.set_tuning("render.mode", old)
+        sc.release()
