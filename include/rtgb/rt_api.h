@@ -179,6 +179,8 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *   "trace.minblocks" 16, 12 (default) or 10: resident 128-thread blocks per
  *                   SM the per-lane caster is compiled for (register budget)
  *   "trace.packet_minblocks"  the same for the packet caster (default 10)
+ *   "trace.host_chunk"  rays per pipelined chunk of rtTraceClosestHost
+ *                   (65536 .. 2^26, default 2^21)
  *   "trace.defer"   1 (default) = 32-ray chunks that fail the packet test are
  *                   listed and cast by a second, per-lane kernel; 0 = cast
  *                   in place by the packet kernel with plain per-lane

@@ -620,9 +620,9 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     std::lock_guard<std::mutex> g(ctx->mu);
     opts = ctx->trace_opts;
   }
-  // Chunks alternate between two streams so the copy of one chunk overlaps
-  // the traversal of the other.
-  const uint32_t chunk = 1u << 20;
+  // Chunks of trace.host_chunk rays alternate between two streams so the
+  // copy of one chunk overlaps the traversal of the other.
+  const uint32_t chunk = opts.host_chunk;
   const size_t io_bytes = (size_t)chunk * (sizeof(rt_ray) + sizeof(rt_hit));
   const size_t chunk_bytes = (trace_chunk_scratch_bytes(chunk) + 255) & ~size_t(255);
   const size_t need = io_bytes + chunk_bytes + raysort_scratch_bytes(chunk);
@@ -740,6 +740,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.packet_minblocks = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.host_chunk") {
+    if (value < 65536 || value > (1 << 26)) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.host_chunk = (uint32_t)value;
+    return RT_SUCCESS;
+  }
   if (k == "trace.defer") {
     if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.defer = (int)value;
@@ -794,6 +799,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.defer") {
     *value = ctx->trace_opts.defer;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.host_chunk") {
+    *value = ctx->trace_opts.host_chunk;
     return RT_SUCCESS;
   }
   if (k == "render.mode") {

@@ -65,6 +65,7 @@ struct TraceOpts {
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
   int packet_minblocks = 10;  // the same for the packet caster
   int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
+  uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
 };
 
 // `counter` is a device word private to this launch (work distribution);
