@@ -166,7 +166,7 @@ def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 30.0):
     dt = time.perf_counter() - t0
     n = len(a) + len(b)
     return {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": thr, "kind": "port",
-            "sample": f"every {stride}th ray of each batch ({n} rays), oracle fp32 culled traversal, "
+            "sample": f"one ray in {stride} of each batch ({n} rays), oracle fp32 culled traversal, "
                       f"{thr} OpenMP threads, {dt:.1f} s"}
 
 
@@ -203,10 +203,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_per_step": f"every {stride}th ray of each batch "
+        "config": {"workload": WORKLOAD, "sample_per_step": f"one ray in {stride} of each batch "
                                                             f"({len(a) + len(b)} rays)"},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": thr, "kind": "port",
-                         "sample": f"every {stride}th ray of each batch, oracle restatement of hit_bvh "
+                         "sample": f"one ray in {stride} of each batch, oracle restatement of hit_bvh "
                                    f"(culled), {thr} OpenMP threads"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference GLSL path unavailable on this box (no graphics stack); its CPU restatement is timed",
