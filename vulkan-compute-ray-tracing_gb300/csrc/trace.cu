@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
       // Inner nodes until this lane holds a leaf or runs out of work.
       while (node >= 0) {
         const float4 *N = bvh + 4ll * node;
-        float4 a = __ldg(N), b = __ldg(N + 1), c = __ldg(N + 2), d = __ldg(N + 3);
+        float4 a, b, c, d;
+        load_node(N, a, b, c, d);
         float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
         float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
         int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
