@@ -1,8 +1,10 @@
 """Test infrastructure (oracle) — NOT part of the product.
 
 ctypes access to the CPU oracle (liboracle.so, built from rt_oracle.cpp) and,
-where it was built, to the reference's own BVH builder (_ref/libref_bvh.so,
-built from the reference's src/ray-tracing/Bvh.h). Only the tests,
+where they were built, to the reference's own BVH builder (_ref/libref_bvh.so,
+built from the reference's src/ray-tracing/Bvh.h) and its own compute shader
+(_ref/libref_shader.so, ray-trace-compute.comp rewritten into C++ by
+glsl2cpp.py). Only the tests,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module,
 and only as the checker / the timed CPU baseline.
 """
@@ -61,6 +63,41 @@ def _p(a):
 
 def ref_available() -> bool:
     return os.path.exists(REF_PATH)
+
+
+REF_SHADER_PATH = os.path.join(HERE, "_ref", "libref_shader.so")
+
+
+def ref_shader_available() -> bool:
+    """True where the recipe compiled the reference's own compute shader."""
+    return os.path.exists(REF_SHADER_PATH)
+
+
+def ref_shader_render(tris, mats, nodes, lights, spheres, cam_pos, width: int, height: int, frames: int,
+                      first_sample: int = 0, lights_len: int = 1, spheres_len: int = 1,
+                      threads: int = 0) -> np.ndarray:
+    """The reference's ray-trace-compute.comp, compiled from its source via
+    glsl2cpp.py, driven frame by frame as src/main.cpp drives it: returns the
+    rgba8 target image after `frames` dispatches as floats (H, W, 4). The
+    bound lengths of the light and sphere arrays default to 1, as the
+    reference application binds them."""
+    lib = ctypes.CDLL(REF_SHADER_PATH)
+    P, U32 = ctypes.c_void_p, ctypes.c_uint32
+    lib.ref_shader_render.restype = ctypes.c_int
+    lib.ref_shader_render.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, P, U32, U32, P, U32, U32, U32, U32, P,
+                                      ctypes.c_int]
+    tris, mats, nodes = (np.ascontiguousarray(a, np.float32) for a in (tris, mats, nodes))
+    lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 2)
+    spheres = np.zeros((1, 8), np.float32) if spheres is None or len(spheres) == 0 else \
+        np.ascontiguousarray(spheres, np.float32)
+    cam = np.ascontiguousarray(cam_pos, np.float32)
+    out = np.zeros((height, width, 4), np.float32)
+    rc = lib.ref_shader_render(_p(tris), len(tris), _p(mats), len(mats), _p(nodes), len(nodes), _p(lights),
+                               len(lights), lights_len, _p(spheres), len(spheres), spheres_len, _p(cam), width,
+                               height, first_sample, frames, _p(out), threads)
+    if rc != 0:
+        raise RuntimeError(f"ref_shader_render failed ({rc})")
+    return out
 
 
 REF_SCENE_DIR = os.path.join(HERE, "_ref", "doge_scene")

@@ -14,9 +14,15 @@ Fixtures:
                   determinism of the generators);
   rand.json       the first values of glibc rand() for a few seeds;
   trace_*.npy     oracle closest hits for small ray sets;
-  render_*.npy    oracle images of small renders.
-The shader-side fixtures come from the oracle (the reference ships no test
-vectors and its GLSL cannot run without a Vulkan stack).
+  render_*.npy    oracle images of small renders;
+  ref_shader_*.npy  rgba8 images made by the REFERENCE's own compute shader
+                  (ray-trace-compute.comp compiled on the host through
+                  oracle/glsl2cpp.py, oracle/_ref/libref_shader.so), driven
+                  frame by frame as src/main.cpp drives it: the pins for the
+                  oracle's shader restatement and the GPU kernels' compat
+                  mode on machines without the reference checkout.
+
+`--ref-shader-only` regenerates just the ref_shader_* fixtures.
 """
 import hashlib
 import json
@@ -63,7 +69,48 @@ def node_rows(nodes: np.ndarray, rows):
     return {int(r): nodes.view(np.uint32)[r, NODE_COLS].tolist() for r in rows}
 
 
+# Reference-shader fixtures: name -> (scene builder, camPos, W, H, frames,
+# lights bound). camPos goes through the shader's own camera (vfov 30,
+# origin = camPos.zxy * (-1, 1, 1), looking down -z).
+def ref_shader_cases():
+    def cornell():
+        t, m, _ = rtgb.gen_cornell(3, 3000, 0)
+        m = m.copy()
+        m[:, 1] = 0.0  # metal fuzz is not part of the reference's material
+        return t, m, np.zeros((1, 8), np.float32)
+    return {
+        "ref_shader_cornell_96x64": (cornell, (0.0, 4.5, 0.0), 96, 64, 3, "one"),
+        "ref_shader_cornell_96x64_lights": (cornell, (0.0, 4.5, 0.0), 96, 64, 2, "all"),
+    }
+
+
+def ref_shader_fixtures():
+    if not oracle.ref_shader_available():
+        raise SystemExit("oracle/_ref/libref_shader.so is missing: run `make -C oracle` with the reference present")
+    meta = {}
+    cases = dict(ref_shader_cases())
+    if oracle.ref_scene_available():
+        cases["ref_shader_doge_128x96"] = (lambda: rtgb.load_reference_scene(oracle.REF_SCENE_DIR),
+                                           rtgb.REFERENCE_CAMERA_POS, 128, 96, 4, "one")
+    for name, (build, cam_pos, W, H, frames, lights_mode) in cases.items():
+        t, m, sph = build()
+        nodes = oracle.ref_build_bvh(t, 1)
+        lights = oracle.lights_from_materials(t, m)
+        img = oracle.ref_shader_render(t, m, nodes, lights, sph, cam_pos, W, H, frames,
+                                       lights_len=1 if lights_mode == "one" else len(lights))
+        q = np.rint(img * 255.0).astype(np.uint8)
+        np.save(os.path.join(HERE, name + ".npy"), q)
+        meta[name] = {"cam_pos": list(map(float, cam_pos)), "width": W, "height": H, "frames": frames,
+                      "lights": lights_mode, "max_bounces": 2}
+        print(name, W, H, frames, float(img[..., :3].mean()))
+    with open(os.path.join(HERE, "ref_shader.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
 def main():
+    if "--ref-shader-only" in sys.argv:
+        ref_shader_fixtures()
+        return
     big = "--no-big" not in sys.argv
     if not oracle.ref_available():
         raise SystemExit("oracle/_ref/libref_bvh.so is missing: run `make -C oracle` with the reference present")
@@ -120,6 +167,7 @@ def main():
     img, _ = oracle.render(t, m, nodes, lights, s, cam, 64, 64, spp=4, max_bounces=8,
                            flags=rtgb.COMPAT_STACK16 | rtgb.COMPAT_LEN1 | rtgb.COMPAT_UNORM8)
     np.save(os.path.join(HERE, "render_cornell_64_compat.npy"), img)
+    ref_shader_fixtures()
     print("golden fixtures written")
 
 

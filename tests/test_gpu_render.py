@@ -262,3 +262,61 @@ def test_partial_tiles_multi_sample_vs_oracle(rt, orc, ctx, mode):
     finally:
         ctx.set_tuning("render.mode", old)
         sc.release()
+
+
+def _ref_fixture(name):
+    import json
+    with open(os.path.join(GOLDEN, "ref_shader.json")) as f:
+        meta = json.load(f)[name]
+    return meta, np.load(os.path.join(GOLDEN, name + ".npy"))
+
+
+def _compat_frames(rt, sc, meta, all_lights):
+    """The GPU kernels in the reference's own configuration, frame by frame."""
+    import torch
+    flags = rt.COMPAT_STACK16 | rt.COMPAT_NO_SPHERES | rt.COMPAT_UNORM8 | (0 if all_lights else rt.COMPAT_LEN1)
+    W, H = meta["width"], meta["height"]
+    sc.set_camera(rt.camera_from_reference(meta["cam_pos"], W, H))
+    acc = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    for s in range(meta["frames"]):
+        sc.render(acc, W, H, spp=1, max_bounces=meta["max_bounces"], sample_index=s, flags=flags)
+    sc.ctx.synchronize()
+    return np.rint(acc.cpu().numpy().astype(np.float64) * 255.0).astype(np.uint8)
+
+
+@pytest.mark.parametrize("name", ["ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights"])
+def test_kernels_match_reference_shader(rt, ctx, name):
+    """Against images made by the reference's own compute shader (compiled on
+    the host from its source): the GPU kernels in compat mode, through the
+    GPU-built Bvh.h tree. Tolerance: CUDA's sinf/cosf and libm's differ in
+    the last ulp, which can move a bounce direction; pixel values are rgba8."""
+    meta, want = _ref_fixture(name)
+    t, m, _ = rt.gen_cornell(3, 3000, 0)
+    m = m.copy()
+    m[:, 1] = 0.0
+    sc = ctx.upload_scene(t, m)
+    try:
+        got = _compat_frames(rt, sc, meta, meta["lights"] == "all")
+    finally:
+        sc.release()
+    exact = (got == want).all(axis=2).mean()
+    err = np.abs(got.astype(np.float64) - want) / 255.0
+    assert exact >= 0.99, exact
+    assert (err.reshape(-1, 4).mean(axis=0) <= TOL).all(), err.reshape(-1, 4).mean(axis=0)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
+                                                    "doge_scene", "buff-doge.obj")),
+                    reason="the reference's demo scene was not copied")
+def test_kernels_match_reference_shader_on_its_scene(rt, orc, ctx):
+    meta, want = _ref_fixture("ref_shader_doge_128x96")
+    tris, mats, sph = rt.load_reference_scene(orc.REF_SCENE_DIR)
+    sc = ctx.upload_scene(tris, mats, spheres=sph)
+    try:
+        got = _compat_frames(rt, sc, meta, False)
+    finally:
+        sc.release()
+    exact = (got == want).all(axis=2).mean()
+    err = np.abs(got.astype(np.float64) - want) / 255.0
+    assert exact >= 0.99, exact
+    assert (err.reshape(-1, 4).mean(axis=0) <= TOL).all(), err.reshape(-1, 4).mean(axis=0)

@@ -1,0 +1,122 @@
+"""The reference's own compute shader as the pin for the shader restatement.
+
+ray-trace-compute.comp is compiled on the host from its source
+(oracle/glsl2cpp.py + oracle/shim/glsl.h -> oracle/_ref/libref_shader.so)
+and driven frame by frame as src/main.cpp drives it: hit_bvh with its
+16-entry stack, NUM_BOUNCES 2, no spheres, lights.length() of the bound
+range, rgba8 target and accumulation images. The oracle's restatement in the
+matching compat mode (RT_COMPAT_STACK16 | LEN1 | NO_SPHERES | UNORM8, two
+bounces, rtCameraFromReference) must equal it byte for byte. The committed
+ref_shader_*.npy fixtures carry the reference's output to machines without
+the checkout, where the oracle is checked against them instead."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+COMPAT = ("COMPAT_STACK16", "COMPAT_LEN1", "COMPAT_NO_SPHERES", "COMPAT_UNORM8")
+
+
+def fixture_meta():
+    with open(os.path.join(GOLDEN, "ref_shader.json")) as f:
+        return json.load(f)
+
+
+def cornell_scene(rt):
+    t, m, _ = rt.gen_cornell(3, 3000, 0)
+    m = m.copy()
+    m[:, 1] = 0.0  # metal fuzz is not part of the reference's material
+    return t, m, np.zeros((1, 8), np.float32)
+
+
+def oracle_frames(rt, orc, t, m, nodes, lights, sph, cam_pos, W, H, frames, all_lights):
+    flags = 0
+    for name in COMPAT:
+        if name == "COMPAT_LEN1" and all_lights:
+            continue
+        flags |= getattr(rt, name)
+    cam = rt.camera_from_reference(cam_pos, W, H).as_array()
+    acc = np.zeros((H, W, 4), np.float32)
+    for s in range(frames):
+        acc, _ = orc.render(t, m, nodes, lights, sph, cam, W, H, spp=1, max_bounces=2, sample_index=s, flags=flags,
+                            accum=acc)
+    return acc
+
+
+def as_u8(img):
+    return np.rint(np.asarray(img, np.float64) * 255.0).astype(np.uint8)
+
+
+@pytest.mark.parametrize("name", ["ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights"])
+def test_oracle_equals_reference_shader_fixture(rt, orc, name):
+    """Runs everywhere: the restatement against the reference's committed output."""
+    meta = fixture_meta()[name]
+    t, m, sph = cornell_scene(rt)
+    nodes, _ = orc.build_bvh(t, 1)
+    lights = orc.lights_from_materials(t, m)
+    got = oracle_frames(rt, orc, t, m, nodes, lights, sph, meta["cam_pos"], meta["width"], meta["height"],
+                        meta["frames"], meta["lights"] == "all")
+    want = np.load(os.path.join(GOLDEN, name + ".npy"))
+    assert np.array_equal(as_u8(got), want)
+    assert want[..., :3].mean() > 10  # a lit image, not an empty one
+
+
+needs_ref_shader = pytest.mark.skipif(
+    not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref", "libref_shader.so")),
+    reason="the reference's shader was not compiled (no reference checkout)")
+
+
+@needs_ref_shader
+@pytest.mark.parametrize("frames,all_lights,first", [(1, False, 0), (3, False, 0), (2, True, 0), (2, False, 5)])
+def test_oracle_equals_reference_shader(rt, orc, frames, all_lights, first):
+    t, m, sph = cornell_scene(rt)
+    nodes = orc.ref_build_bvh(t, 1)
+    lights = orc.lights_from_materials(t, m)
+    W, H, cam_pos = 64, 64, (0.3, 4.0, -0.2)
+    want = orc.ref_shader_render(t, m, nodes, lights, sph, cam_pos, W, H, frames, first_sample=first,
+                                 lights_len=len(lights) if all_lights else 1)
+    flags = 0
+    for name in COMPAT:
+        if name == "COMPAT_LEN1" and all_lights:
+            continue
+        flags |= getattr(rt, name)
+    cam = rt.camera_from_reference(cam_pos, W, H).as_array()
+    acc = np.zeros((H, W, 4), np.float32)
+    for s in range(first, first + frames):
+        acc, _ = orc.render(t, m, nodes, lights, sph, cam, W, H, spp=1, max_bounces=2, sample_index=s, flags=flags,
+                            accum=acc)
+    assert np.array_equal(as_u8(acc), as_u8(want))
+
+
+@needs_ref_shader
+def test_reference_shader_fixtures_are_current(rt, orc):
+    """The committed fixtures are what the compiled reference shader makes."""
+    meta = fixture_meta()
+    for name in ("ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights"):
+        mt = meta[name]
+        t, m, sph = cornell_scene(rt)
+        nodes = orc.ref_build_bvh(t, 1)
+        lights = orc.lights_from_materials(t, m)
+        img = orc.ref_shader_render(t, m, nodes, lights, sph, mt["cam_pos"], mt["width"], mt["height"],
+                                    mt["frames"], lights_len=len(lights) if mt["lights"] == "all" else 1)
+        assert np.array_equal(as_u8(img), np.load(os.path.join(GOLDEN, name + ".npy")))
+
+
+@needs_ref_shader
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
+                                                    "doge_scene", "buff-doge.obj")),
+                    reason="the reference's demo scene was not copied")
+def test_oracle_equals_reference_shader_on_its_scene(rt, orc):
+    """The reference's own scene, camera and shader against the restatement."""
+    tris, mats, sph = rt.load_reference_scene(orc.REF_SCENE_DIR)
+    nodes = orc.ref_build_bvh(tris, 1)
+    lights = orc.lights_from_materials(tris, mats)
+    meta = fixture_meta()["ref_shader_doge_128x96"]
+    W, H, F = meta["width"], meta["height"], meta["frames"]
+    want = orc.ref_shader_render(tris, mats, nodes, lights, sph, rt.REFERENCE_CAMERA_POS, W, H, F)
+    got = oracle_frames(rt, orc, tris, mats, nodes, lights, sph, rt.REFERENCE_CAMERA_POS, W, H, F, False)
+    assert np.array_equal(as_u8(got), as_u8(want))
+    assert np.array_equal(as_u8(want), np.load(os.path.join(GOLDEN, "ref_shader_doge_128x96.npy")))
