@@ -100,6 +100,21 @@ def ref_shader_render(tris, mats, nodes, lights, spheres, cam_pos, width: int, h
     return out
 
 
+def ref_shader_trace(tris, nodes, rays, threads: int = 0) -> np.ndarray:
+    """The reference shader's own hit_bvh for each ray (its 16-entry stack and
+    fixed t range): hit distance or -1 per ray."""
+    lib = ctypes.CDLL(REF_SHADER_PATH)
+    P, U32 = ctypes.c_void_p, ctypes.c_uint32
+    lib.ref_shader_trace.restype = ctypes.c_int
+    lib.ref_shader_trace.argtypes = [P, U32, P, U32, P, U32, P, ctypes.c_int]
+    tris, nodes, rays = (np.ascontiguousarray(a, np.float32) for a in (tris, nodes, rays))
+    t = np.zeros(len(rays), np.float32)
+    rc = lib.ref_shader_trace(_p(tris), len(tris), _p(nodes), len(nodes), _p(rays), len(rays), _p(t), threads)
+    if rc != 0:
+        raise RuntimeError(f"ref_shader_trace failed ({rc})")
+    return t
+
+
 REF_SCENE_DIR = os.path.join(HERE, "_ref", "doge_scene")
 
 

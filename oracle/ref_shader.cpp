@@ -30,6 +30,38 @@ GlslArray<sphere> spheres;
 
 static vec3 v3(const float *p) { return vec3(p[0], p[1], p[2]); }
 
+static std::vector<triangle> g_T;
+static std::vector<bvhNode> g_B;
+
+// Binds the triangle and node buffers only (closest-hit casting).
+static void bind_geometry(const rt_triangle *tris, uint32_t nt, const rt_bvh_node *nodes, uint32_t nn) {
+  g_T.resize(nt);
+  for (uint32_t i = 0; i < nt; i++)
+    g_T[i] = triangle{v3(tris[i].v0), v3(tris[i].v1), v3(tris[i].v2), tris[i].material_index};
+  g_B.resize(nn);
+  for (uint32_t i = 0; i < nn; i++)
+    g_B[i] = bvhNode{v3(nodes[i].min), v3(nodes[i].max), nodes[i].left, nodes[i].right, nodes[i].object};
+  triangles = GlslArray<triangle>{g_T.data(), (int)nt};
+  bvh = GlslArray<bvhNode>{g_B.data(), (int)nn};
+}
+
+// The shader's own closest-hit traversal (hit_bvh: 16-entry stack, every
+// hit box pushes both children, t in (0.001, 10000)) for each ray; t_out
+// receives the hit distance or -1. Used as the reference's CPU timing.
+extern "C" int ref_shader_trace(const rt_triangle *tris, uint32_t nt, const rt_bvh_node *nodes, uint32_t nn,
+                                const rt_ray *rays, uint32_t n, float *t_out, int threads) {
+  if (!tris || !nodes || !rays || !t_out) return 1;
+  bind_geometry(tris, nt, nodes, nn);
+  if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+  for (long i = 0; i < (long)n; i++) {
+    ray r{v3(rays[i].o), v3(rays[i].d)};
+    hit_record rec{};
+    t_out[i] = hit_bvh(r, rec) ? rec.t : -1.0f;
+  }
+  return 0;
+}
+
 extern "C" int ref_shader_render(const rt_triangle *tris, uint32_t nt, const rt_material *mats, uint32_t nm,
                                  const rt_bvh_node *nodes, uint32_t nn, const rt_light *ls, uint32_t nl,
                                  uint32_t lights_len, const rt_sphere *sph, uint32_t ns, uint32_t spheres_len,

@@ -120,3 +120,23 @@ def test_oracle_equals_reference_shader_on_its_scene(rt, orc):
     got = oracle_frames(rt, orc, tris, mats, nodes, lights, sph, rt.REFERENCE_CAMERA_POS, W, H, F, False)
     assert np.array_equal(as_u8(got), as_u8(want))
     assert np.array_equal(as_u8(want), np.load(os.path.join(GOLDEN, "ref_shader_doge_128x96.npy")))
+
+
+@needs_ref_shader
+@pytest.mark.parametrize("level,seed", [(5, 2), (6, 3)])
+def test_literal_traversal_equals_reference_hit_bvh(rt, orc, level, seed):
+    """The shader's own hit_bvh (16-entry stack, both children pushed, t in
+    (0.001, 10000)) against the oracle's literal traversal: same hits, same
+    t bits, including the rays its stack truncates on these 16- and 18-level
+    trees."""
+    tris = rt.gen_icosphere(seed, level)
+    nodes = orc.ref_build_bvh(tris, 1)
+    cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 64, 64)
+    rays = np.concatenate([rt.gen_camera_rays(cam, 64, 64), rt.gen_random_rays(5, 8192)])
+    rays[:, 3] = 0.001
+    rays[:, 7] = 10000.0
+    t = orc.ref_shader_trace(tris, nodes, rays)
+    lit = orc.trace(tris, nodes, rays, mode=1, stack_size=16)
+    hit = lit.view(np.int32)[:, 0] >= 0
+    assert np.array_equal(t >= 0, hit)
+    assert np.array_equal(t[hit].view(np.uint32), lit[hit, 1].view(np.uint32))
