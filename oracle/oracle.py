@@ -38,6 +38,7 @@ def _load():
         "oracle_lights_from_materials": (U32, [P, U32, P, U32, P]),
         "oracle_camera_from_reference": (None, [P, U32, U32, P]),
         "oracle_denoise": (None, [P, U32, U32, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P]),
+        "oracle_hit_records": (None, [P, U32, P, U32, P, U32, P, U32, U32, P]),
         "oracle_trace": (I32, [P, U32, P, U32, P, U32, I32, I32, D, P, P, I32]),
         "oracle_trace_f64": (I32, [P, U32, P, U32, P, U32, P, P, I32]),
         "oracle_render": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
@@ -113,6 +114,37 @@ def ref_shader_trace(tris, nodes, rays, threads: int = 0) -> np.ndarray:
     if rc != 0:
         raise RuntimeError(f"ref_shader_trace failed ({rc})")
     return t
+
+
+def hit_records(tris, nodes, spheres, rays, flags: int = 0) -> np.ndarray:
+    """Shading hit records (n, 10): hit, t, p, normal, material (uint bits),
+    back face (int bits) — the `closest` step of ray_color under `flags`."""
+    tris, nodes, rays = (np.ascontiguousarray(a, np.float32) for a in (tris, nodes, rays))
+    sph = np.zeros((1, 8), np.float32) if spheres is None or len(spheres) == 0 else \
+        np.ascontiguousarray(spheres, np.float32)
+    ns = 0 if spheres is None else len(spheres)
+    out = np.zeros((len(rays), 10), np.float32)
+    LIB.oracle_hit_records(_p(tris), len(tris), _p(nodes), len(nodes), _p(sph), ns, _p(rays), len(rays), flags,
+                           _p(out))
+    return out
+
+
+def ref_shader_hit_records(tris, nodes, spheres, rays, use_scene: bool, spheres_len: int) -> np.ndarray:
+    """The reference shader's own hit_scene (use_scene) or hit_bvh records,
+    laid out as hit_records()."""
+    lib = ctypes.CDLL(REF_SHADER_PATH)
+    P, U32 = ctypes.c_void_p, ctypes.c_uint32
+    lib.ref_shader_hit_records.restype = ctypes.c_int
+    lib.ref_shader_hit_records.argtypes = [P, U32, P, U32, P, U32, U32, P, U32, ctypes.c_int, P, ctypes.c_int]
+    tris, nodes, rays = (np.ascontiguousarray(a, np.float32) for a in (tris, nodes, rays))
+    sph = np.zeros((1, 8), np.float32) if spheres is None or len(spheres) == 0 else \
+        np.ascontiguousarray(spheres, np.float32)
+    out = np.zeros((len(rays), 10), np.float32)
+    rc = lib.ref_shader_hit_records(_p(tris), len(tris), _p(nodes), len(nodes), _p(sph), len(sph), spheres_len,
+                                    _p(rays), len(rays), 1 if use_scene else 0, _p(out), 0)
+    if rc != 0:
+        raise RuntimeError(f"ref_shader_hit_records failed ({rc})")
+    return out
 
 
 REF_SCENE_DIR = os.path.join(HERE, "_ref", "doge_scene")

@@ -62,6 +62,41 @@ extern "C" int ref_shader_trace(const rt_triangle *tris, uint32_t nt, const rt_b
   return 0;
 }
 
+// The shader's own hit records: hit_scene (comp:222-246: every triangle in a
+// linear loop, then every bound sphere with `closest` reset to t_max) or
+// hit_bvh (comp:262-311), per ray; out as oracle_hit_records (10 floats).
+extern "C" int ref_shader_hit_records(const rt_triangle *tris, uint32_t nt, const rt_bvh_node *nodes, uint32_t nn,
+                                      const rt_sphere *sph, uint32_t ns, uint32_t spheres_len, const rt_ray *rays,
+                                      uint32_t n, int use_scene, float *out, int threads) {
+  if (!tris || !nodes || !rays || !out || spheres_len > ns) return 1;
+  bind_geometry(tris, nt, nodes, nn);
+  static std::vector<sphere> S;
+  S.resize(ns > 0 ? ns : 1);
+  for (uint32_t i = 0; i < ns; i++)
+    S[i] = sphere{vec4(sph[i].s[0], sph[i].s[1], sph[i].s[2], sph[i].s[3]), sph[i].material_index};
+  spheres = GlslArray<sphere>{S.data(), (int)spheres_len};
+  ubo.numTriangles = nt;
+  if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+  for (long i = 0; i < (long)n; i++) {
+    ray r{v3(rays[i].o), v3(rays[i].d)};
+    hit_record rec{};
+    bool h = use_scene ? hit_scene(r, rec) : hit_bvh(r, rec);
+    float *o = out + 10 * i;
+    o[0] = h ? 1.0f : 0.0f;
+    o[1] = rec.t;
+    o[2] = rec.p.x;
+    o[3] = rec.p.y;
+    o[4] = rec.p.z;
+    o[5] = rec.normal.x;
+    o[6] = rec.normal.y;
+    o[7] = rec.normal.z;
+    std::memcpy(o + 8, &rec.materialIndex, 4);
+    std::memcpy(o + 9, &rec.backFaceInt, 4);
+  }
+  return 0;
+}
+
 extern "C" int ref_shader_render(const rt_triangle *tris, uint32_t nt, const rt_material *mats, uint32_t nm,
                                  const rt_bvh_node *nodes, uint32_t nn, const rt_light *ls, uint32_t nl,
                                  uint32_t lights_len, const rt_sphere *sph, uint32_t ns, uint32_t spheres_len,

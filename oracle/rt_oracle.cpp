@@ -726,6 +726,42 @@ int oracle_render_f64(const rt_triangle *tris, uint32_t ntris, const rt_material
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
 
+// The shading hit record of each ray (the `closest` step of ray_color under
+// `flags`: BVH traversal, then the sphere pass of the flags' mode), in fp32.
+// out gets 10 floats per ray: hit (0/1), t, p.xyz, normal.xyz, material
+// index (uint bits), back-face flag (int bits). Rays are rt_ray records
+// (only origin and direction are used; t runs over (0.001, 10000) as in the
+// shader).
+void oracle_hit_records(const rt_triangle *tris, uint32_t ntris, const rt_bvh_node *nodes, uint32_t nnodes,
+                        const rt_sphere *spheres, uint32_t nspheres, const rt_ray *rays, uint32_t n, uint32_t flags,
+                        float *out) {
+  Scene sc{tris, ntris, nullptr, 0, nodes, nnodes, nullptr, 0, spheres, nspheres};
+  Effective ef;
+  bool len1 = (flags & RT_COMPAT_LEN1) != 0;
+  ef.nlights = 0;
+  ef.nspheres = len1 ? std::min<uint32_t>(nspheres, 1u) : nspheres;
+  ef.sphere_mode = (flags & RT_COMPAT_NO_SPHERES) ? 0 : ((flags & RT_COMPAT_SPHERE_OVERRIDE) ? 2 : 1);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long i = 0; i < (long)n; i++) {
+    Shader<float> sh{sc, ef, flags, Rng{0}};
+    Hit<float> rec{};
+    uint64_t seg = 0;
+    V3<float> ro = ld3<float>(rays[i].o), rd = ld3<float>(rays[i].d);
+    bool hit = sh.closest(ro, rd, rec, seg);
+    float *o = out + 10 * i;
+    o[0] = hit ? 1.0f : 0.0f;
+    o[1] = rec.t;
+    o[2] = rec.p.x;
+    o[3] = rec.p.y;
+    o[4] = rec.p.z;
+    o[5] = rec.normal.x;
+    o[6] = rec.normal.y;
+    o[7] = rec.normal.z;
+    std::memcpy(o + 8, &rec.mat, 4);
+    std::memcpy(o + 9, &rec.back, 4);
+  }
+}
+
 // smartDeNoise (post-process-shader.frag:26-68) over an RGBA32F image, as a
 // texel-space restatement: taps at (px + x, py + y) fetched bilinearly with
 // REPEAT wrap (the reference's sampler, src/memory/Image.cpp:353-357), every

@@ -140,3 +140,26 @@ def test_literal_traversal_equals_reference_hit_bvh(rt, orc, level, seed):
     hit = lit.view(np.int32)[:, 0] >= 0
     assert np.array_equal(t >= 0, hit)
     assert np.array_equal(t[hit].view(np.uint32), lit[hit, 1].view(np.uint32))
+
+
+@needs_ref_shader
+@pytest.mark.parametrize("seed,n_soup,n_spheres", [(4, 2000, 6), (5, 500, 16), (6, 8000, 3)])
+def test_hit_records_equal_reference(rt, orc, seed, n_soup, n_spheres):
+    """Full shading hit records (t, p with its 1e-4 offset, normal, material,
+    back face) against the shader's own functions:
+      * hit_scene (every triangle in index order, then the spheres with
+        `closest` reset) = the default culled traversal with
+        RT_COMPAT_SPHERE_OVERRIDE: an exact-t tie goes to the lower triangle
+        index in both, which the linear loop's strict `t < closest` implies;
+      * hit_bvh = the literal 16-entry traversal with RT_COMPAT_NO_SPHERES."""
+    t, m, s = rt.gen_cornell(seed, n_soup, n_spheres, 0.2, 1.0)
+    nodes = orc.ref_build_bvh(t, 1)
+    cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 64, 64)
+    rays = np.concatenate([rt.gen_camera_rays(cam, 64, 64), rt.gen_random_rays(7, 8192, -4.0, 4.0)])
+    for use_scene, flags in ((True, rt.COMPAT_SPHERE_OVERRIDE), (False, rt.COMPAT_NO_SPHERES | rt.COMPAT_STACK16)):
+        ref = orc.ref_shader_hit_records(t, nodes, s, rays, use_scene, len(s))
+        got = orc.hit_records(t, nodes, s, rays, flags)
+        hit = ref[:, 0] > 0
+        assert hit.mean() > 0.5
+        assert np.array_equal(ref[:, 0], got[:, 0])
+        assert np.array_equal(ref[hit].view(np.uint32), got[hit].view(np.uint32))
