@@ -21,6 +21,11 @@ is never committed:
   * local scalars declared without an initialiser get `{}` (GLSL leaves
     them undefined; where the shader reads one, the value never reaches
     its output);
+  * vector constructors `vecN(a, b, c)` become `vecN{a, b, c}`: GLSL
+    evaluates call arguments left to right (GLSL 4.50, 6.1.1), C++ leaves
+    the order of function arguments unspecified but fixes it for braced
+    initialisers (random_in_unit_sphere calls random() three times inside
+    one constructor);
   * main() becomes glsl_main(); random() becomes glsl_random() (POSIX has a
     random()); imageSize() becomes glsl_imageSize() (main declares a local
     of that name, which GLSL scopes after its initialiser and C++ before).
@@ -49,6 +54,26 @@ def strip_comments(src: str) -> str:
     return re.sub(r"//[^\n]*", "", src)
 
 
+def braced_constructors(src: str) -> str:
+    """vec2/vec3/vec4/ivec2 ( ... ) -> { ... }, with nested parentheses."""
+    out, i = [], 0
+    pat = re.compile(r"\b(?:vec[234]|ivec2)\s*\(")
+    while True:
+        m = pat.search(src, i)
+        if not m:
+            out.append(src[i:])
+            return "".join(out)
+        out.append(src[i:m.end() - 1] + "{")
+        depth, j = 1, m.end()
+        while depth:
+            c = src[j]
+            depth += (c == "(") - (c == ")")
+            j += 1
+        inner = braced_constructors(src[m.end():j - 1])
+        out.append(inner + "}")
+        i = j
+
+
 def translate(src: str) -> str:
     src = strip_comments(src)
     src = re.sub(r"^\s*#version[^\n]*\n", "", src, flags=re.M)
@@ -69,6 +94,7 @@ def translate(src: str) -> str:
     src = re.sub(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?)(?![fF\w.])", r"\1f", src)
     # Swizzles.
     src = re.sub(r"\.(xyz|zxy|xy|rgba|rgb)\b(?!\s*\()", r".\1()", src)
+    src = braced_constructors(src)
     # Renames.
     src = re.sub(r"\brandom\b(?=\s*\()", "glsl_random", src)
     src = re.sub(r"\bimageSize\b(?=\s*\()", "glsl_imageSize", src)

@@ -67,6 +67,7 @@ def ref_available() -> bool:
 
 
 REF_SHADER_PATH = os.path.join(HERE, "_ref", "libref_shader.so")
+REF_SHADER_SIMPLE_PATH = os.path.join(HERE, "_ref", "libref_shader_simple.so")
 
 
 def ref_shader_available() -> bool:
@@ -76,13 +77,14 @@ def ref_shader_available() -> bool:
 
 def ref_shader_render(tris, mats, nodes, lights, spheres, cam_pos, width: int, height: int, frames: int,
                       first_sample: int = 0, lights_len: int = 1, spheres_len: int = 1,
-                      threads: int = 0) -> np.ndarray:
+                      threads: int = 0, simple: bool = False) -> np.ndarray:
     """The reference's ray-trace-compute.comp, compiled from its source via
     glsl2cpp.py, driven frame by frame as src/main.cpp drives it: returns the
     rgba8 target image after `frames` dispatches as floats (H, W, 4). The
     bound lengths of the light and sphere arrays default to 1, as the
-    reference application binds them."""
-    lib = ctypes.CDLL(REF_SHADER_PATH)
+    reference application binds them. `simple` runs
+    ray-trace-compute-simple.comp instead."""
+    lib = ctypes.CDLL(REF_SHADER_SIMPLE_PATH if simple else REF_SHADER_PATH)
     P, U32 = ctypes.c_void_p, ctypes.c_uint32
     lib.ref_shader_render.restype = ctypes.c_int
     lib.ref_shader_render.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, P, U32, U32, P, U32, U32, U32, U32, P,

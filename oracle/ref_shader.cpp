@@ -1,8 +1,9 @@
 // Test infrastructure (oracle) — NOT part of the product.
 //
-// Runs the reference's own compute shader (ray-trace-compute.comp, rewritten
-// into C++ by glsl2cpp.py and included here as SHADER_GEN) on the host the
-// way the reference application drives it (src/main.cpp:166-261):
+// Runs the reference's own compute shader (ray-trace-compute.comp, or with
+// REF_SHADER_SIMPLE ray-trace-compute-simple.comp; rewritten into C++ by
+// glsl2cpp.py and included here as SHADER_GEN) on the host the way the
+// reference application drives it (src/main.cpp:166-261):
 //   per frame: the UBO gets currentSample, every pixel runs main() with its
 //   gl_GlobalInvocationID (rngState re-initialised per invocation, as GLSL
 //   evaluates global initialisers per invocation), the shader writes the

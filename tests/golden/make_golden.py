@@ -18,7 +18,8 @@ Fixtures:
   ref_shader_*.npy  rgba8 images made by the REFERENCE's own compute shader
                   (ray-trace-compute.comp compiled on the host through
                   oracle/glsl2cpp.py, oracle/_ref/libref_shader.so), driven
-                  frame by frame as src/main.cpp drives it: the pins for the
+                  frame by frame as src/main.cpp drives it (the _simple_ one
+                  from ray-trace-compute-simple.comp): the pins for the
                   oracle's shader restatement and the GPU kernels' compat
                   mode on machines without the reference checkout.
 
@@ -70,8 +71,10 @@ def node_rows(nodes: np.ndarray, rows):
 
 
 # Reference-shader fixtures: name -> (scene builder, camPos, W, H, frames,
-# lights bound). camPos goes through the shader's own camera (vfov 30,
-# origin = camPos.zxy * (-1, 1, 1), looking down -z).
+# lights bound, shader). camPos goes through the shader's own camera (vfov
+# 30, origin = camPos.zxy * (-1, 1, 1), looking down -z). Shader "full" is
+# ray-trace-compute.comp (NUM_BOUNCES 2), "simple" is
+# ray-trace-compute-simple.comp (NUM_BOUNCES 4, hemisphere scattering).
 def ref_shader_cases():
     def cornell():
         t, m, _ = rtgb.gen_cornell(3, 3000, 0)
@@ -79,8 +82,9 @@ def ref_shader_cases():
         m[:, 1] = 0.0  # metal fuzz is not part of the reference's material
         return t, m, np.zeros((1, 8), np.float32)
     return {
-        "ref_shader_cornell_96x64": (cornell, (0.0, 4.5, 0.0), 96, 64, 3, "one"),
-        "ref_shader_cornell_96x64_lights": (cornell, (0.0, 4.5, 0.0), 96, 64, 2, "all"),
+        "ref_shader_cornell_96x64": (cornell, (0.0, 4.5, 0.0), 96, 64, 3, "one", "full"),
+        "ref_shader_cornell_96x64_lights": (cornell, (0.0, 4.5, 0.0), 96, 64, 2, "all", "full"),
+        "ref_shader_simple_cornell_96x64": (cornell, (0.0, 4.5, 0.0), 96, 64, 4, "one", "simple"),
     }
 
 
@@ -91,17 +95,18 @@ def ref_shader_fixtures():
     cases = dict(ref_shader_cases())
     if oracle.ref_scene_available():
         cases["ref_shader_doge_128x96"] = (lambda: rtgb.load_reference_scene(oracle.REF_SCENE_DIR),
-                                           rtgb.REFERENCE_CAMERA_POS, 128, 96, 4, "one")
-    for name, (build, cam_pos, W, H, frames, lights_mode) in cases.items():
+                                           rtgb.REFERENCE_CAMERA_POS, 128, 96, 4, "one", "full")
+    for name, (build, cam_pos, W, H, frames, lights_mode, shader) in cases.items():
         t, m, sph = build()
         nodes = oracle.ref_build_bvh(t, 1)
         lights = oracle.lights_from_materials(t, m)
         img = oracle.ref_shader_render(t, m, nodes, lights, sph, cam_pos, W, H, frames,
-                                       lights_len=1 if lights_mode == "one" else len(lights))
+                                       lights_len=1 if lights_mode == "one" else len(lights),
+                                       simple=shader == "simple")
         q = np.rint(img * 255.0).astype(np.uint8)
         np.save(os.path.join(HERE, name + ".npy"), q)
         meta[name] = {"cam_pos": list(map(float, cam_pos)), "width": W, "height": H, "frames": frames,
-                      "lights": lights_mode, "max_bounces": 2}
+                      "lights": lights_mode, "max_bounces": 4 if shader == "simple" else 2, "shader": shader}
         print(name, W, H, frames, float(img[..., :3].mean()))
     with open(os.path.join(HERE, "ref_shader.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

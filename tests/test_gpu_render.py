@@ -275,6 +275,8 @@ def _compat_frames(rt, sc, meta, all_lights):
     """The GPU kernels in the reference's own configuration, frame by frame."""
     import torch
     flags = rt.COMPAT_STACK16 | rt.COMPAT_NO_SPHERES | rt.COMPAT_UNORM8 | (0 if all_lights else rt.COMPAT_LEN1)
+    if meta.get("shader") == "simple":
+        flags |= rt.SHADE_SIMPLE
     W, H = meta["width"], meta["height"]
     sc.set_camera(rt.camera_from_reference(meta["cam_pos"], W, H))
     acc = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
@@ -284,7 +286,8 @@ def _compat_frames(rt, sc, meta, all_lights):
     return np.rint(acc.cpu().numpy().astype(np.float64) * 255.0).astype(np.uint8)
 
 
-@pytest.mark.parametrize("name", ["ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights"])
+@pytest.mark.parametrize("name", ["ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights",
+                                  "ref_shader_simple_cornell_96x64"])
 def test_kernels_match_reference_shader(rt, ctx, name):
     """Against images made by the reference's own compute shader (compiled on
     the host from its source): the GPU kernels in compat mode, through the

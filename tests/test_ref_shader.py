@@ -8,7 +8,9 @@ range, rgba8 target and accumulation images. The oracle's restatement in the
 matching compat mode (RT_COMPAT_STACK16 | LEN1 | NO_SPHERES | UNORM8, two
 bounces, rtCameraFromReference) must equal it byte for byte. The committed
 ref_shader_*.npy fixtures carry the reference's output to machines without
-the checkout, where the oracle is checked against them instead."""
+the checkout, where the oracle is checked against them instead. The same
+holds for ray-trace-compute-simple.comp (oracle/_ref/libref_shader_simple.so)
+and the RT_SHADE_SIMPLE mode."""
 import json
 import os
 
@@ -32,17 +34,22 @@ def cornell_scene(rt):
     return t, m, np.zeros((1, 8), np.float32)
 
 
-def oracle_frames(rt, orc, t, m, nodes, lights, sph, cam_pos, W, H, frames, all_lights):
-    flags = 0
+def compat_flags(rt, all_lights, simple=False):
+    flags = rt.SHADE_SIMPLE if simple else 0
     for name in COMPAT:
         if name == "COMPAT_LEN1" and all_lights:
             continue
         flags |= getattr(rt, name)
+    return flags
+
+
+def oracle_frames(rt, orc, t, m, nodes, lights, sph, cam_pos, W, H, frames, all_lights, simple=False):
+    flags = compat_flags(rt, all_lights, simple)
     cam = rt.camera_from_reference(cam_pos, W, H).as_array()
     acc = np.zeros((H, W, 4), np.float32)
     for s in range(frames):
-        acc, _ = orc.render(t, m, nodes, lights, sph, cam, W, H, spp=1, max_bounces=2, sample_index=s, flags=flags,
-                            accum=acc)
+        acc, _ = orc.render(t, m, nodes, lights, sph, cam, W, H, spp=1, max_bounces=4 if simple else 2,
+                            sample_index=s, flags=flags, accum=acc)
     return acc
 
 
@@ -50,15 +57,20 @@ def as_u8(img):
     return np.rint(np.asarray(img, np.float64) * 255.0).astype(np.uint8)
 
 
-@pytest.mark.parametrize("name", ["ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights"])
+CORNELL_FIXTURES = ["ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights", "ref_shader_simple_cornell_96x64"]
+
+
+@pytest.mark.parametrize("name", CORNELL_FIXTURES)
 def test_oracle_equals_reference_shader_fixture(rt, orc, name):
     """Runs everywhere: the restatement against the reference's committed output."""
     meta = fixture_meta()[name]
+    simple = meta.get("shader") == "simple"
+    assert meta["max_bounces"] == (4 if simple else 2)
     t, m, sph = cornell_scene(rt)
     nodes, _ = orc.build_bvh(t, 1)
     lights = orc.lights_from_materials(t, m)
     got = oracle_frames(rt, orc, t, m, nodes, lights, sph, meta["cam_pos"], meta["width"], meta["height"],
-                        meta["frames"], meta["lights"] == "all")
+                        meta["frames"], meta["lights"] == "all", simple)
     want = np.load(os.path.join(GOLDEN, name + ".npy"))
     assert np.array_equal(as_u8(got), want)
     assert want[..., :3].mean() > 10  # a lit image, not an empty one
@@ -78,11 +90,7 @@ def test_oracle_equals_reference_shader(rt, orc, frames, all_lights, first):
     W, H, cam_pos = 64, 64, (0.3, 4.0, -0.2)
     want = orc.ref_shader_render(t, m, nodes, lights, sph, cam_pos, W, H, frames, first_sample=first,
                                  lights_len=len(lights) if all_lights else 1)
-    flags = 0
-    for name in COMPAT:
-        if name == "COMPAT_LEN1" and all_lights:
-            continue
-        flags |= getattr(rt, name)
+    flags = compat_flags(rt, all_lights)
     cam = rt.camera_from_reference(cam_pos, W, H).as_array()
     acc = np.zeros((H, W, 4), np.float32)
     for s in range(first, first + frames):
@@ -91,18 +99,46 @@ def test_oracle_equals_reference_shader(rt, orc, frames, all_lights, first):
     assert np.array_equal(as_u8(acc), as_u8(want))
 
 
+needs_ref_shader_simple = pytest.mark.skipif(
+    not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref", "libref_shader_simple.so")),
+    reason="the reference's simple shader was not compiled (no reference checkout)")
+
+
 @needs_ref_shader
+@needs_ref_shader_simple
 def test_reference_shader_fixtures_are_current(rt, orc):
-    """The committed fixtures are what the compiled reference shader makes."""
+    """The committed fixtures are what the compiled reference shaders make."""
     meta = fixture_meta()
-    for name in ("ref_shader_cornell_96x64", "ref_shader_cornell_96x64_lights"):
+    for name in CORNELL_FIXTURES:
         mt = meta[name]
         t, m, sph = cornell_scene(rt)
         nodes = orc.ref_build_bvh(t, 1)
         lights = orc.lights_from_materials(t, m)
         img = orc.ref_shader_render(t, m, nodes, lights, sph, mt["cam_pos"], mt["width"], mt["height"],
-                                    mt["frames"], lights_len=len(lights) if mt["lights"] == "all" else 1)
+                                    mt["frames"], lights_len=len(lights) if mt["lights"] == "all" else 1,
+                                    simple=mt.get("shader") == "simple")
         assert np.array_equal(as_u8(img), np.load(os.path.join(GOLDEN, name + ".npy")))
+
+
+@needs_ref_shader_simple
+@pytest.mark.parametrize("frames,first,cam_pos", [(1, 0, (0.3, 4.0, -0.2)), (3, 2, (0.0, 4.5, 0.0))])
+def test_simple_shading_equals_reference_simple_shader(rt, orc, frames, first, cam_pos):
+    """ray-trace-compute-simple.comp (hit_bvh, NUM_BOUNCES 4, every bounce
+    scatters into the normal's hemisphere with a normalised
+    random_in_unit_sphere, emitters end the path) against the restatement's
+    RT_SHADE_SIMPLE mode, byte for byte."""
+    t, m, sph = cornell_scene(rt)
+    nodes = orc.ref_build_bvh(t, 1)
+    lights = orc.lights_from_materials(t, m)
+    W, H = 64, 48
+    want = orc.ref_shader_render(t, m, nodes, lights, sph, cam_pos, W, H, frames, first_sample=first, simple=True)
+    cam = rt.camera_from_reference(cam_pos, W, H).as_array()
+    acc = np.zeros((H, W, 4), np.float32)
+    for s in range(first, first + frames):
+        acc, _ = orc.render(t, m, nodes, lights, sph, cam, W, H, spp=1, max_bounces=4, sample_index=s,
+                            flags=compat_flags(rt, False, True), accum=acc)
+    assert np.array_equal(as_u8(acc), as_u8(want))
+    assert as_u8(want)[..., :3].mean() > 5
 
 
 @needs_ref_shader
