@@ -185,6 +185,14 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   listed and cast by a second, per-lane kernel; 0 = cast
  *                   in place by the packet kernel with plain per-lane
  *                   traversal (no postponed leaves)
+ *   "trace.wide"    1 (default) = rays of the per-lane kernel (chunks that
+ *                   fail the packet test) are cast over the scene's 8-wide
+ *                   fold of the same tree: each step tests all eight child
+ *                   boxes of a node, and leaves are tested 32 at a time by
+ *                   the whole warp from a shared pool; 0 = the binary layout
+ *                   with postponed leaves. Results are identical either way
+ *   "trace.wide_minblocks" 8, 6 (default) or 5: resident 128-thread blocks
+ *                   per SM the 8-wide caster is compiled for
  *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from render.wavefront_pixels up;
@@ -206,7 +214,7 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value);
 
 /* Autotuner (no counterpart in the reference, whose launch shape is fixed at
  * compile time). Times the closest-hit launch shapes on the caller's own
- * device rays (coordinate descent over trace.defer, trace.spec,
+ * device rays (coordinate descent over trace.wide, trace.wide_minblocks, trace.defer, trace.spec,
  * trace.minblocks, trace.packet_minblocks, trace.sort; `reps` timed casts
  * per candidate after one warm-up) and keeps the fastest. Hits are identical
  * in every shape; d_hits receives them. The rates before and after tuning

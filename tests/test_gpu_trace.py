@@ -201,27 +201,28 @@ def test_invalid_scenes_are_rejected(rt, ctx):
     sc.release()
 
 
-KEYS = ("trace.refill", "trace.sort", "trace.packet", "trace.spec")
+KEYS = ("trace.refill", "trace.sort", "trace.packet", "trace.spec", "trace.wide")
 
 
-@pytest.mark.parametrize("refill,sort,packet,spec", [
-    (1, 0, 0, 0), (4, 0, 0, 0), (16, 0, 0, 0), (32, 1, 0, 0), (4, 1, 0, 0), (32, 1, 1, 0), (32, 0, 1, 0),
-    (32, 0, 0, 1), (32, 1, 0, 1), (32, 1, 1, 1)])
-def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec):
+@pytest.mark.parametrize("refill,sort,packet,spec,wide", [
+    (1, 0, 0, 0, 0), (4, 0, 0, 0, 0), (16, 0, 0, 0, 0), (32, 1, 0, 0, 0), (4, 1, 0, 0, 0), (32, 1, 1, 0, 0),
+    (32, 0, 1, 0, 0), (32, 0, 0, 1, 0), (32, 1, 0, 1, 0), (32, 1, 1, 1, 0), (32, 0, 0, 0, 1), (32, 1, 0, 0, 1),
+    (32, 0, 1, 0, 1), (32, 1, 1, 1, 1)])
+def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wide):
     """Every launch shape of the caster (refill threshold, Morton order,
-    packet traversal of coherent warps, postponed leaves) returns the same
-    results in input order, bit for bit: the visiting order differs between
-    shapes, and equal-t candidates are resolved by leaf index, not by the
-    order met."""
+    packet traversal of coherent warps, postponed leaves, the 8-wide tree
+    with the warp leaf pool) returns the same results in input order, bit for bit:
+    the visiting order differs between shapes, and equal-t candidates are
+    resolved by leaf index, not by the order met."""
     tris, sc = mesh_scene(rt, ctx, 6, 7)
     try:
         cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 256, 200)
         rays = np.concatenate([rt.gen_camera_rays(cam, 256, 200), rt.gen_random_rays(11, 40000)])
         old = [ctx.get_tuning(k) for k in KEYS]
-        for k, v in zip(KEYS, (32, 0, 0, 0)):
+        for k, v in zip(KEYS, (32, 0, 0, 0, 0)):
             ctx.set_tuning(k, v)
         base = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
-        for k, v in zip(KEYS, (refill, sort, packet, spec)):
+        for k, v in zip(KEYS, (refill, sort, packet, spec, wide)):
             ctx.set_tuning(k, v)
         try:
             got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
@@ -246,8 +247,9 @@ def test_single_triangle_scene(rt, orc, ctx):
         cam = rt.camera_look_at([0, 0, -14], [0, -4, 0], [0, 1, 0], 60.0, 64, 64)
         rays = rt.gen_camera_rays(cam, 64, 64)
         want = orc.trace(t, sc.bvh(), rays)
-        for spec in (0, 1):
+        for spec, wide in ((0, 0), (1, 0), (0, 1)):
             ctx.set_tuning("trace.spec", spec)
+            ctx.set_tuning("trace.wide", wide)
             got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
             np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
     finally:
@@ -302,7 +304,7 @@ def test_alt_tree_mode_same_hits(rt, orc, ctx, builder):
 def test_autotune_trace_keeps_hits(rt, orc, ctx):
     """The autotuner's candidates are timing choices only: after tuning, the
     hits equal the ones cast with the settings it started from."""
-    keys = ("trace.defer", "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort")
+    keys = ("trace.wide", "trace.wide_minblocks", "trace.defer", "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort")
     old = [ctx.get_tuning(k) for k in keys]
     tris, sc = mesh_scene(rt, ctx, 6, 3)
     try:
@@ -315,7 +317,8 @@ def test_autotune_trace_keeps_hits(rt, orc, ctx):
         before, after = rt.autotune_trace(sc, d_rays, len(rays), d_hits, reps=1)
         assert before > 0 and after > 0
         for k in keys:
-            assert ctx.get_tuning(k) in ((16, 12, 10) if "minblocks" in k else (0, 1))
+            assert ctx.get_tuning(k) in ((8, 6, 5) if k == "trace.wide_minblocks" else
+                                         (16, 12, 10) if "minblocks" in k else (0, 1))
         got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     finally:

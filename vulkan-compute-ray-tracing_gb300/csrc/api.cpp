@@ -137,7 +137,7 @@ uint32_t check_tree(const rt_bvh_node *nodes, uint32_t nn, uint32_t ntris, std::
 }
 
 struct SlabLayout {
-  size_t tris, mats, lights, spheres, nodes, bvh2, tpre, leaf, total;
+  size_t tris, mats, lights, spheres, nodes, bvh2, tpre, leaf, bvh8, total;
 };
 
 SlabLayout slab_layout(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
@@ -151,7 +151,8 @@ SlabLayout slab_layout(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
   L.bvh2 = L.nodes + align256(sizeof(rt_bvh_node) * nnodes);
   L.tpre = L.bvh2 + align256(64ull * ninner);
   L.leaf = L.tpre + align256(48ull * nt);
-  L.total = L.leaf + align256(4ull * nt);
+  L.bvh8 = L.leaf + align256(4ull * nt);
+  L.total = L.bvh8 + align256(256ull * bvh8_capacity(nt));
   return L;
 }
 
@@ -358,7 +359,7 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   // One slab per scene.
   SlabLayout L = slab_layout(nt, nm, nl, ns);
   size_t off_tris = L.tris, off_mats = L.mats, off_lights = L.lights, off_spheres = L.spheres, off_nodes = L.nodes,
-         off_bvh2 = L.bvh2, off_tpre = L.tpre, off_leaf = L.leaf, total = L.total;
+         off_bvh2 = L.bvh2, off_tpre = L.tpre, off_leaf = L.leaf, off_bvh8 = L.bvh8, total = L.total;
   {
     std::lock_guard<std::mutex> g(ctx->mu);
     if (ctx->used + total > ctx->budget)
@@ -466,6 +467,15 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
       d.root_hi[k] = root.max[k];
     }
     d.root_ref = (root.left != -1) ? 0 : ~0;
+  }
+  // The 8-wide fold of the same tree.
+  {
+    char errbuf[128] = {0};
+    cudaError_t be = build_bvh8(d, (float4 *)(slab + off_bvh8), bvh8_capacity(nt), &d.n8, &d.levels8, errbuf,
+                                sizeof(errbuf), st);
+    if (be != cudaSuccess && errbuf[0]) return abort_upload(fail(ctx, RT_ERR_INTERNAL, "%s", errbuf));
+    UCK(be, "bvh8");
+    d.bvh8 = (const float4 *)(slab + off_bvh8);
   }
 #undef UCK
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -750,6 +760,16 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.defer = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.wide") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.wide = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.wide_minblocks") {
+    if (value != 8 && value != 6 && value != 5) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.wide_minblocks = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.wavefront_pixels") {
     if (value < 1 || value > (1ll << 31)) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.wavefront_pixels = (uint64_t)value;
@@ -799,6 +819,14 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.defer") {
     *value = ctx->trace_opts.defer;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.wide") {
+    *value = ctx->trace_opts.wide;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.wide_minblocks") {
+    *value = ctx->trace_opts.wide_minblocks;
     return RT_SUCCESS;
   }
   if (k == "trace.host_chunk") {

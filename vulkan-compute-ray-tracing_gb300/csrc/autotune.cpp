@@ -2,7 +2,7 @@
 // rtAutotuneRender in rt_api.h). Every knob it touches leaves results
 // unchanged (hits and images are identical in every shape), so tuning is a
 // pure timing search on the caller's own workload:
-//   closest hit  coordinate descent over trace.defer, trace.spec,
+//   closest hit  coordinate descent over trace.wide, trace.wide_minblocks, trace.defer, trace.spec,
 //                trace.minblocks, trace.packet_minblocks and trace.sort,
 //                each candidate timed with CUDA events over `reps` casts
 //                after one warm-up cast;
@@ -87,7 +87,9 @@ rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, 
     const char *key;
     std::vector<int64_t> values;
   };
-  const Knob knobs[] = {{"trace.defer", {1, 0}},
+  const Knob knobs[] = {{"trace.wide", {1, 0}},
+                        {"trace.wide_minblocks", {8, 6, 5}},
+                        {"trace.defer", {1, 0}},
                         {"trace.spec", {1, 0}},
                         {"trace.minblocks", {16, 12, 10}},
                         {"trace.packet_minblocks", {16, 12, 10}},

@@ -1,0 +1,206 @@
+// 8-wide traversal tree (bvh8) collapsed from the children-pair layout.
+//
+// The tree is the reference's (or the selected builder's) binary tree with
+// levels folded together; no box is recomputed or moved. Each bvh8 node
+// holds up to eight children: starting from one inner node's two children,
+// the inner child with the largest surface area is replaced by its own two
+// children until there are eight or only leaves are left (greedy collapse
+// as in Wald et al., "Getting Rid of Packets", RT 2008, and Ylitie et al.,
+// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+// BVHs", HPG 2017). A node with fewer than eight children therefore holds
+// leaves only, which bounds the node count by (4n - 1) / 7 for n leaves.
+//
+// Layout: a node is 8 slots of 32 bytes (256 bytes, one 256-bit load per
+// slot): (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref, 0). ref >= 0 is a
+// bvh8 node, ~k a leaf (tpre record k, as in bvh2), and an empty slot has
+// every bound +inf, which every slab test misses (entry +inf, or exit -inf
+// for a negative direction component), with ref INT_MIN. Nodes are numbered
+// breadth first, level by level; the children of one node are consecutive.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdio>
+#include <cstring>
+
+#include "rt_internal.h"
+
+namespace rtgb {
+namespace {
+
+struct Slot {
+  float lo[3], hi[3];
+  int32_t ref;
+};
+
+__device__ __forceinline__ float slot_area(const Slot &s) {
+  float dx = s.hi[0] - s.lo[0], dy = s.hi[1] - s.lo[1], dz = s.hi[2] - s.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// The two children of bvh2 pair p.
+__device__ __forceinline__ void load_pair(const float4 *__restrict__ bvh2, int32_t p, Slot &c0, Slot &c1) {
+  const float4 *N = bvh2 + 4ll * p;
+  const float4 a = N[0], b = N[1], c = N[2], d = N[3];
+  c0.lo[0] = a.x, c0.hi[0] = a.y, c0.lo[1] = a.z, c0.hi[1] = a.w, c0.lo[2] = c.x, c0.hi[2] = c.y;
+  c1.lo[0] = b.x, c1.hi[0] = b.y, c1.lo[1] = b.z, c1.hi[1] = b.w, c1.lo[2] = c.z, c1.hi[2] = c.w;
+  c0.ref = __float_as_int(d.x);
+  c1.ref = __float_as_int(d.y);
+}
+
+// One frontier node per thread: bvh2 pair frontier[f] becomes bvh8 node
+// base + f. inner_cnt[f] receives its number of inner children.
+__global__ void k_collapse8(const float4 *__restrict__ bvh2, uint32_t n_pairs, const int32_t *__restrict__ frontier,
+                            uint32_t count, uint32_t base, float4 *__restrict__ bvh8, uint32_t *__restrict__ inner_cnt,
+                            uint32_t *__restrict__ err) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= count) return;
+  Slot S[8];
+  int cnt = 0;
+  const int32_t p0 = frontier[f];
+  if (p0 < 0 || (uint32_t)p0 >= n_pairs) {
+    atomicOr(err, 1u);
+  } else {
+    load_pair(bvh2, p0, S[0], S[1]);
+    cnt = 2;
+    while (cnt < 8) {
+      int pick = -1;
+      float best = -1.0f;
+      for (int i = 0; i < cnt; i++) {
+        if (S[i].ref < 0) continue;
+        const float a = slot_area(S[i]);
+        if (a > best) {
+          best = a;
+          pick = i;
+        }
+      }
+      if (pick < 0) break;
+      const int32_t p = S[pick].ref;
+      if ((uint32_t)p >= n_pairs) {
+        atomicOr(err, 1u);
+        break;
+      }
+      load_pair(bvh2, p, S[pick], S[cnt]);
+      cnt++;
+    }
+  }
+  float4 *o = bvh8 + 16ull * (base + f);
+  const float inf = __int_as_float(0x7f800000);
+  uint32_t inner = 0;
+  for (int s = 0; s < 8; s++) {
+    if (s < cnt) {
+      o[2 * s] = make_float4(S[s].lo[0], S[s].lo[1], S[s].lo[2], S[s].hi[0]);
+      o[2 * s + 1] = make_float4(S[s].hi[1], S[s].hi[2], __int_as_float(S[s].ref), 0.0f);
+      inner += S[s].ref >= 0 ? 1u : 0u;
+    } else {
+      o[2 * s] = make_float4(inf, inf, inf, inf);
+      o[2 * s + 1] = make_float4(inf, inf, __int_as_float(INT_MIN), 0.0f);
+    }
+  }
+  inner_cnt[f] = inner;
+}
+
+// Numbers the inner children of the level's nodes (next_base + offs[f] + i)
+// and lists their bvh2 pairs as the next frontier.
+__global__ void k_link8(uint32_t count, uint32_t base, uint32_t next_base, const uint32_t *__restrict__ offs,
+                        float4 *__restrict__ bvh8, int32_t *__restrict__ next_frontier, uint32_t cap,
+                        uint32_t *__restrict__ err) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= count) return;
+  float4 *o = bvh8 + 16ull * (base + f);
+  uint32_t r = offs[f];
+  for (int s = 0; s < 8; s++) {
+    float4 w = o[2 * s + 1];
+    const int32_t ref = __float_as_int(w.z);
+    if (ref < 0) continue;
+    if (next_base + r >= cap) {
+      atomicOr(err, 2u);
+      return;
+    }
+    next_frontier[r] = ref;
+    w.z = __int_as_float((int32_t)(next_base + r));
+    o[2 * s + 1] = w;
+    r++;
+  }
+}
+
+}  // namespace
+
+uint32_t bvh8_capacity(uint32_t ntris) { return ntris ? (uint32_t)((4ull * ntris + 6) / 7 + 1) : 0; }
+
+cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
+                       char *errbuf, size_t errlen, cudaStream_t st) {
+  *n8_out = 0;
+  *levels_out = 0;
+  if (d.ntris == 0 || cap == 0 || !bvh8) return cudaErrorInvalidValue;
+  if (d.root_ref < 0) {
+    // One triangle: a single node with the root leaf in slot 0.
+    auto bits = [](int32_t i) {
+      float f;
+      std::memcpy(&f, &i, 4);
+      return f;
+    };
+    float4 h[16];
+    const float inf = bits(0x7f800000);
+    for (int s = 0; s < 8; s++) {
+      h[2 * s] = make_float4(inf, inf, inf, inf);
+      h[2 * s + 1] = make_float4(inf, inf, bits(INT_MIN), 0.0f);
+    }
+    h[0] = make_float4(d.root_lo[0], d.root_lo[1], d.root_lo[2], d.root_hi[0]);
+    h[1] = make_float4(d.root_hi[1], d.root_hi[2], bits(d.root_ref), 0.0f);
+    cudaError_t e = cudaMemcpyAsync(bvh8, h, sizeof(h), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    *n8_out = 1;
+    *levels_out = 1;
+    return cudaSuccess;
+  }
+  const uint32_t n_pairs = d.ntris - 1;
+  // Scratch: two frontiers, counts, offsets (cap words each), scan sums, error word.
+  const size_t words = 4ull * cap + cap / 1024 + 8;
+  uint32_t *scr = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&scr, 4 * words, st);
+  if (e != cudaSuccess) return e;
+  int32_t *fr = (int32_t *)scr, *fr_next = (int32_t *)(scr + cap);
+  uint32_t *cnt = scr + 2ull * cap, *offs = scr + 3ull * cap, *errw = scr + 4ull * cap;
+  uint32_t *sums = errw + 4;
+  e = cudaMemsetAsync(errw, 0, 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(fr, 0, 4, st);  // the root pair is bvh2 record 0
+  uint32_t count = 1, base = 0, levels = 0, bad = 0;
+  while (e == cudaSuccess && count > 0) {
+    if (base + count > cap) {
+      bad = 4;
+      break;
+    }
+    const uint32_t grid = (count + 255) / 256;
+    k_collapse8<<<grid, 256, 0, st>>>(d.bvh2, n_pairs, fr, count, base, bvh8, cnt, errw);
+    e = exclusive_scan_u32(cnt, offs, sums, count, st);
+    if (e != cudaSuccess) break;
+    k_link8<<<grid, 256, 0, st>>>(count, base, base + count, offs, bvh8, fr_next, cap, errw);
+    e = cudaGetLastError();
+    uint32_t tail[3] = {0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[0], offs + count - 1, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[1], cnt + count - 1, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[2], errw, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) break;
+    levels++;
+    base += count;
+    count = tail[0] + tail[1];
+    bad = tail[2];
+    if (bad) break;
+    int32_t *t = fr;
+    fr = fr_next;
+    fr_next = t;
+  }
+  cudaFreeAsync(scr, st);
+  if (e != cudaSuccess) return e;
+  if (bad) {
+    snprintf(errbuf, errlen, "bvh8 collapse: %s", bad & 4 ? "node capacity exceeded" : "bad child reference");
+    return cudaErrorInvalidValue;
+  }
+  *n8_out = base;
+  *levels_out = levels;
+  return cudaSuccess;
+}
+
+}  // namespace rtgb

@@ -31,6 +31,10 @@ enum : uint32_t {
 //           (ray-trace-compute.comp:157-173), computed once with the same
 //           rounding.
 //   leaf_tri  original triangle index of leaf k.
+//   bvh8    the same tree with levels folded into nodes of up to eight
+//           children (bvh8.cu): 8 slots of 32 B, (lo.xyz, hi.x),
+//           (hi.yz, ref, 0), breadth-first numbered, root node 0; leaf refs
+//           are the bvh2 ones (~k). Used by the per-lane 8-wide caster.
 struct DevScene {
   const rt_triangle *tris;
   const rt_material *mats;
@@ -45,7 +49,16 @@ struct DevScene {
   int32_t root_ref;
   uint32_t ntris, nmats, nlights, nspheres, nnodes;
   uint32_t depth;
+  const float4 *bvh8;
+  uint32_t n8, levels8;  // bvh8 nodes and levels (0 when absent)
 };
+
+// ---------------------------------------------------------------- bvh8.cu
+// Node capacity the collapse may need for `ntris` leaves: (4n - 1) / 7 + 1.
+uint32_t bvh8_capacity(uint32_t ntris);
+// Folds d.bvh2 into bvh8 (capacity `cap` nodes); synchronises `st`.
+cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
+                       char *errbuf, size_t errlen, cudaStream_t st);
 
 // ---------------------------------------------------------------- relayout.cu
 // Exclusive scan of n words (in may equal out); `sums` needs ceil(n/1024).
@@ -65,6 +78,8 @@ struct TraceOpts {
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
   int packet_minblocks = 10;  // the same for the packet caster
   int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
+  int wide = 1;     // 1: per-lane chunks are cast over bvh8 with a warp leaf pool (k_trace_wide)
+  int wide_minblocks = 6;  // resident 128-thread blocks per SM k_trace_wide is compiled for (8, 6 or 5)
   uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
 };
 

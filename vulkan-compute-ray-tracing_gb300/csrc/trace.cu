@@ -2,8 +2,9 @@
 // work from a global counter. The default whole-warp cast runs two kernels
 // per batch: k_trace_packets takes 32 consecutive rays (Morton order) per
 // warp and traverses coherent ones as a packet, listing the rest, and
-// k_trace_lanes casts the listed chunks one ray per lane with postponed
-// leaves. k_trace is the per-lane refill form (a warp claims new rays as
+// k_trace_wide casts the listed chunks one ray per lane over the 8-wide
+// tree with a shared leaf pool (k_trace_lanes: the same over the binary
+// layout with postponed leaves). k_trace is the per-lane refill form (a warp claims new rays as
 // lanes finish), k_trace_literal16 the shader's literal traversal.
 //
 // The hit is chosen with the reference's fp32 arithmetic (traverse.cuh).
@@ -270,6 +271,267 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_lanes(DevScene sc, 
   }
 }
 
+// One bvh8 slot (32 bytes) in one 256-bit load: (lo.x, lo.y, lo.z, hi.x),
+// (hi.y, hi.z, ref, 0). Nodes are 256 bytes and the slab is 256-byte
+// aligned, so every slot is 32-byte aligned.
+__device__ __forceinline__ void load_slot8(const float4 *P, float4 &a, float4 &b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(P));
+}
+
+// Ordered keys for (t, triangle) pairs: ord_f maps fp32 to uint32 so that
+// unsigned order equals float order (-0 is first mapped to +0 by the
+// callers, which compare it equal to +0 as floats do).
+__device__ __forceinline__ uint32_t ord_f(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_inv(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// triIntersect of test_triangle on one precomputed record, without the
+// acceptance rule: true when tmin < t <= closest and the hit lies inside.
+__device__ __forceinline__ bool tri_candidate(const float4 *__restrict__ tpre, int k, f3 o, f3 d, float tmin,
+                                              float closest, float &t, float &u, float &v) {
+  const float4 *T = tpre + 3ll * k;
+  const float4 t0 = __ldg(T), t1 = __ldg(T + 1), t2 = __ldg(T + 2);
+  const f3 v0 = mk3(t0.x, t0.y, t0.z), n = mk3(t0.w, t1.x, t1.y);
+  const f3 a = mk3(t1.z, t1.w, t2.x), b = mk3(t2.y, t2.z, t2.w);
+  const f3 p = sub3(v0, o);
+  const float idet = __fdiv_rn(1.0f, dot3(d, n));
+  t = __fmul_rn(dot3(n, p), idet);
+  if (!(t > tmin && t <= closest)) return false;
+  const f3 q = cross3(p, d);
+  u = __fmul_rn(dot3(q, b), idet);
+  v = __fmul_rn(dot3(q, a), idet);
+  return !(u < 0.0f || u > 1.0f || v < 0.0f || __fadd_rn(u, v) > 1.0f);
+}
+
+constexpr int kPool = 512;       // leaf pool entries per warp (power of two)
+constexpr int kWideRefill = 8;   // idle lanes that trigger a fetch of new rays
+
+// One ray per lane over bvh8 (Ylitie et al., HPG 2017, without the node
+// compression): a step tests all eight child slots of the lane's node (eight
+// independent 256-bit loads), ranks the inner children that are hit by
+// entry distance (pairwise compares), descends into the nearest and pushes
+// the rest onto the lane's stack in near-to-far order. Leaves that are hit
+// go to the warp's FIFO leaf pool in shared memory as (leaf, lane) entries;
+// whenever 32 are pooled, or a lane has run out of nodes with entries still
+// pooled, all 32 lanes test one pooled triangle each against the owning
+// lane's ray (kept in shared memory), so triangle tests run with every lane
+// busy whatever the rays' phases. Each ray's closest hit is one 64-bit key
+// (ordered t, triangle index) lowered with a shared-memory atomicMin: a
+// candidate wins when t is smaller, or equal with a lower triangle index —
+// the acceptance rule of test_triangle, independent of the order in which
+// leaves are tested. The winner of a round stores its t, u, v. A ray is done
+// when it has no node, an empty stack, and the pool has moved past its last
+// entry. Idle lanes claim new rays (slots of the listed chunks, or of the
+// whole batch) once kWideRefill of them are idle.
+template <int STACK, bool REFINE, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, const float4 *__restrict__ rays,
+                                                               uint32_t n, int4 *__restrict__ hits,
+                                                               uint32_t *__restrict__ counter, uint32_t *err,
+                                                               const uint32_t *__restrict__ perm,
+                                                               const uint32_t *__restrict__ list,
+                                                               const uint32_t *__restrict__ list_count) {
+  __shared__ float4 s_ray[kTraceBlock / 32][32][2];
+  __shared__ unsigned long long s_key[kTraceBlock / 32][32];
+  __shared__ float4 s_hit[kTraceBlock / 32][32];
+  __shared__ uint32_t s_pool[kTraceBlock / 32][kPool];
+  uint32_t lane;
+  asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+  const uint32_t warp = threadIdx.x >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  float4(*ray_s)[2] = s_ray[warp];
+  volatile unsigned long long *key_v = s_key[warp];
+  unsigned long long *key_a = s_key[warp];
+  float4 *hit_s = s_hit[warp];
+  uint32_t *pool = s_pool[warp];
+  const float INF = __int_as_float(0x7f800000);
+  const uint32_t total = list ? min(*list_count, (n + 31) / 32) * 32u : n;
+  const float4 *__restrict__ bvh8 = sc.bvh8;
+  const int n8 = (int)sc.n8, ntris = (int)sc.ntris;
+  const uint32_t step_cap = sc.n8 + 16u;
+
+  int stack[STACK];
+  int ref[8];
+  TraceRay r = make_ray(mk3(0.0f, 0.0f, 0.0f), mk3(1.0f, 0.0f, 0.0f), 0.0f);
+  int node = -1, sp = 0, ray_i = -1;
+  uint32_t steps = 0, mlp1 = 0, head = 0, tail = 0;
+  bool exhausted = false;
+  for (;;) {
+    // A ray with no node, an empty stack and its last pooled leaf tested.
+    if (ray_i >= 0 && node < 0 && sp == 0 && (int)(head - mlp1) >= 0) {
+      const unsigned long long key = key_v[lane];
+      const float tmax = ray_s[lane][1].w;
+      int4 h = make_int4(-1, 0, 0, 0);
+      if ((uint32_t)(key >> 32) != ord_f(__fadd_rn(tmax, 0.0f))) {
+        const int tri = (int)(uint32_t)key;
+        const float4 w = hit_s[lane];
+        float t = w.x, u = w.y, v = w.z;
+        if (REFINE) refine_fp64(sc.tris, tri, r.o, r.d, t, u, v);
+        h = make_int4(tri, __float_as_int(t), __float_as_int(u), __float_as_int(v));
+      }
+      hits[ray_i] = h;
+      ray_i = -1;
+    }
+    // Idle lanes claim new rays.
+    const uint32_t idle = __ballot_sync(0xffffffffu, ray_i < 0);
+    if (!exhausted && __popc(idle) >= kWideRefill) {
+      const uint32_t cnt = __popc(idle), leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(counter, cnt);
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + cnt >= total) exhausted = true;
+      if (ray_i < 0) {
+        const uint32_t slot = base + __popc(idle & lt_mask);
+        if (slot < total) {
+          const uint32_t ray = list ? __ldg(list + (slot >> 5)) + (slot & 31u) : slot;
+          if (ray < n) {
+            const uint32_t i = perm ? __ldg(perm + ray) : ray;
+            const float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
+            ray_s[lane][0] = r0;
+            ray_s[lane][1] = r1;
+            key_v[lane] = (unsigned long long)ord_f(__fadd_rn(r1.w, 0.0f)) << 32;
+            r = make_ray(mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), r0.w);
+            ray_i = (int)i;
+            sp = 0;
+            steps = 0;
+            mlp1 = head;
+            const float root = slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1],
+                                          sc.root_lo[2], sc.root_hi[2], r1.w);
+            node = root < INF ? 0 : -1;
+          }
+        }
+      }
+    }
+    if (exhausted && __all_sync(0xffffffffu, ray_i < 0)) return;
+    __syncwarp();
+
+    // One node per lane that holds one.
+    uint32_t leafmask = 0;
+    if (ray_i >= 0 && node >= 0) {
+      const float closest = ord_inv((uint32_t)(key_v[lane] >> 32));
+      const float4 *N = bvh8 + 16ll * node;
+      uint32_t key[8];
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        float4 a, b;
+        load_slot8(N + 2 * s, a, b);
+        ref[s] = __float_as_int(b.z);
+        const float t = slab_enter(r, a.x, a.w, a.y, b.x, a.z, b.y, closest);
+        const bool hit = t < INF;
+        key[s] = (hit && ref[s] >= 0) ? ((__float_as_uint(t) & ~7u) | (uint32_t)s) : 0xffffffffu;
+        if (hit && ref[s] < 0) leafmask |= 1u << s;
+      }
+      int rk[8];
+      int cnt = 0;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        rk[s] = 0;
+        cnt += key[s] != 0xffffffffu ? 1 : 0;
+      }
+#pragma unroll
+      for (int s = 1; s < 8; s++) {
+#pragma unroll
+        for (int q = 0; q < s; q++) {
+          const bool lt = key[q] < key[s];
+          rk[s] += lt ? 1 : 0;
+          rk[q] += lt ? 0 : 1;
+        }
+      }
+      int next = -1;
+      if (cnt > 0 && sp + cnt - 1 > STACK) {
+        atomicOr(err, KERR_STACK_OVERFLOW);
+        sp = 0;
+      } else {
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+          if (key[s] == 0xffffffffu) continue;
+          if (rk[s] == 0) next = ref[s];
+          else stack[sp + cnt - 1 - rk[s]] = ref[s];
+        }
+        sp += cnt > 0 ? cnt - 1 : 0;
+      }
+      node = next;
+      if (node >= n8 || ++steps > step_cap) {
+        atomicOr(err, node >= n8 ? KERR_BAD_INDEX : KERR_TIMEOUT);
+        node = -1;
+        sp = 0;
+      }
+    }
+    if (ray_i >= 0 && node < 0 && sp > 0) {
+      node = stack[--sp];
+      if (node < 0 || node >= n8) {
+        atomicOr(err, KERR_BAD_INDEX);
+        node = -1;
+        sp = 0;
+      }
+    }
+
+    // Pool this step's leaves (warp-wide exclusive prefix of the counts).
+    const uint32_t c = __popc(leafmask);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t added = __shfl_sync(0xffffffffu, incl, 31);
+    if (c) {
+      uint32_t pos = tail + incl - c;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        if (!((leafmask >> s) & 1u)) continue;
+        int k = ~ref[s];
+        if (k >= ntris) {
+          atomicOr(err, KERR_BAD_INDEX);
+          k = 0;
+        }
+        pool[pos & (kPool - 1)] = ((uint32_t)k << 5) | lane;
+        pos++;
+      }
+      mlp1 = pos;
+    }
+    tail += added;
+    __syncwarp();
+
+    // Leaf rounds: 32 pooled leaves at a time, oldest first.
+    for (;;) {
+      const bool waiting = ray_i >= 0 && node < 0 && sp == 0 && (int)(head - mlp1) < 0;
+      if (!__any_sync(0xffffffffu, waiting) && tail - head < 32u) break;
+      const uint32_t cnt = min(tail - head, 32u);
+      bool acc = false;
+      unsigned long long cand = 0;
+      uint32_t owner = 0;
+      float ct = 0.0f, cu = 0.0f, cv = 0.0f;
+      if (lane < cnt) {
+        const uint32_t e = pool[(head + lane) & (kPool - 1)];
+        owner = e & 31u;
+        const int k = (int)(e >> 5);
+        const float4 q0 = ray_s[owner][0], q1 = ray_s[owner][1];
+        const unsigned long long cur = key_v[owner];
+        if (tri_candidate(sc.tpre, k, mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), q0.w,
+                          ord_inv((uint32_t)(cur >> 32)), ct, cu, cv)) {
+          const unsigned long long key =
+              ((unsigned long long)ord_f(__fadd_rn(ct, 0.0f)) << 32) | (uint32_t)__ldg(sc.leaf_tri + k);
+          if (key < cur) {
+            acc = true;
+            cand = key;
+            atomicMin(key_a + owner, key);
+          }
+        }
+      }
+      __syncwarp();
+      if (acc && key_v[owner] == cand) hit_s[owner] = make_float4(ct, cu, cv, 0.0f);
+      __syncwarp();
+      head += cnt;
+    }
+  }
+}
+
 // RT_COMPAT_STACK16: the shader's literal traversal, one thread per ray.
 __global__ void __launch_bounds__(kTraceBlock) k_trace_literal16(DevScene sc, const float4 *__restrict__ rays,
                                                                  uint32_t n, int4 *__restrict__ hits) {
@@ -305,6 +567,17 @@ cudaError_t launch_lanes(const DevScene &sc, const float4 *rays, uint32_t n, int
 }
 
 template <int STACK, bool REFINE>
+cudaError_t launch_wide(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
+                        uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
+                        int minblocks, cudaStream_t st) {
+  auto kern = minblocks >= 8 ? k_trace_wide<STACK, REFINE, 8>
+              : minblocks >= 6 ? k_trace_wide<STACK, REFINE, 6>
+                               : k_trace_wide<STACK, REFINE, 5>;
+  kern<<<persistent_grid(kern, n), kTraceBlock, 0, st>>>(sc, rays, n, hits, counter, err, perm, list, list_count);
+  return cudaGetLastError();
+}
+
+template <int STACK, bool REFINE>
 cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
                            uint32_t *err, const TraceOpts &opts, const uint32_t *perm, uint32_t *chunk_scratch,
                            cudaStream_t st) {
@@ -326,6 +599,16 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
       list = chunk_scratch + 64;
       list_count = chunk_scratch;
       lane_counter = chunk_scratch + 1;
+    }
+    if (opts.wide && sc.bvh8 && sc.levels8 >= 1 && sc.ntris < (1u << 27)) {
+      // The stack holds at most 7 entries per level above the last.
+      const uint32_t need = 7u * (sc.levels8 - 1);
+      if (need <= 64)
+        return launch_wide<64, REFINE>(sc, r4, n, h4, lane_counter, err, perm, list, list_count,
+                                       opts.wide_minblocks, st);
+      if (need <= 128)
+        return launch_wide<128, REFINE>(sc, r4, n, h4, lane_counter, err, perm, list, list_count,
+                                        opts.wide_minblocks, st);
     }
     if (opts.minblocks >= 16)
       return launch_lanes<STACK, REFINE, 16>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec, st);
