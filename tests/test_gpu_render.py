@@ -127,26 +127,32 @@ def test_render_without_camera_is_an_error(rt, ctx):
 @pytest.mark.parametrize("flags,spheres,spp", [(0, 6, 3), ("LEN1", 6, 2), ("SPHERE_OVERRIDE", 6, 1),
                                                ("NO_SPHERES", 0, 2), ("UNORM8", 3, 3), ("SHADE_SIMPLE", 3, 1)])
 def test_wavefront_equals_megakernel(rt, ctx, flags, spheres, spp):
-    """The wavefront split (with per-bounce Morton reordering) gives the
-    megakernel's image bit for bit, and counts the same segments."""
+    """The wavefront split (with per-bounce Morton reordering, bounce rays
+    cast in place or by the 8-wide caster) gives the megakernel's image bit
+    for bit, and counts the same segments."""
     import torch
     f = 0 if flags == 0 else (getattr(rt, "COMPAT_" + flags, None) or getattr(rt, flags))
     t, m, s, sc = cornell(rt, ctx, n_soup=5000, n_spheres=spheres, seed=6)
+    keys = ("render.mode", "trace.wide", "trace.wide_min_tris")
     try:
         W, H = 160, 120
         cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
         out = {}
-        old = ctx.get_tuning("render.mode")
+        old = [ctx.get_tuning(k) for k in keys]
         try:
-            for mode in (0, 1):
-                ctx.set_tuning("render.mode", mode)
+            for shape in ((0, 0, 0), (1, 0, 0), (1, 1, 0)):
+                for k, v in zip(keys, shape):
+                    ctx.set_tuning(k, v)
                 ctx.segments(reset=True)
-                out[mode] = (gpu_render(sc, cam, W, H, spp=spp, max_bounces=7, sample_index=2, flags=f),
-                             ctx.segments(reset=True))
+                out[shape] = (gpu_render(sc, cam, W, H, spp=spp, max_bounces=7, sample_index=2, flags=f),
+                              ctx.segments(reset=True))
         finally:
-            ctx.set_tuning("render.mode", old)
-        assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
-        assert out[0][1] == out[1][1]
+            for k, v in zip(keys, old):
+                ctx.set_tuning(k, v)
+        base = out[(0, 0, 0)]
+        for shape in ((1, 0, 0), (1, 1, 0)):
+            assert np.array_equal(base[0].view(np.uint32), out[shape][0].view(np.uint32)), shape
+            assert base[1] == out[shape][1], shape
     finally:
         sc.release()
 

@@ -215,6 +215,8 @@ def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wid
     the visiting order differs between shapes, and equal-t candidates are
     resolved by leaf index, not by the order met."""
     tris, sc = mesh_scene(rt, ctx, 6, 7)
+    old_min = ctx.get_tuning("trace.wide_min_tris")
+    ctx.set_tuning("trace.wide_min_tris", 0)  # this 81,920-triangle mesh takes the 8-wide caster too
     try:
         cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 256, 200)
         rays = np.concatenate([rt.gen_camera_rays(cam, 256, 200), rt.gen_random_rays(11, 40000)])
@@ -234,6 +236,7 @@ def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wid
         assert np.array_equal(host.view(np.uint32), dev_default.view(np.uint32))
         assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
     finally:
+        ctx.set_tuning("trace.wide_min_tris", old_min)
         sc.release()
 
 
@@ -243,6 +246,8 @@ def test_single_triangle_scene(rt, orc, ctx):
     t = t[:1].copy()
     sc = ctx.upload_scene(t, m)
     old = [ctx.get_tuning(k) for k in KEYS]
+    old_min = ctx.get_tuning("trace.wide_min_tris")
+    ctx.set_tuning("trace.wide_min_tris", 0)
     try:
         cam = rt.camera_look_at([0, 0, -14], [0, -4, 0], [0, 1, 0], 60.0, 64, 64)
         rays = rt.gen_camera_rays(cam, 64, 64)
@@ -255,6 +260,7 @@ def test_single_triangle_scene(rt, orc, ctx):
     finally:
         for k, v in zip(KEYS, old):
             ctx.set_tuning(k, v)
+        ctx.set_tuning("trace.wide_min_tris", old_min)
         sc.release()
 
 

@@ -471,8 +471,8 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   // The 8-wide fold of the same tree.
   {
     char errbuf[128] = {0};
-    cudaError_t be = build_bvh8(d, (float4 *)(slab + off_bvh8), bvh8_capacity(nt), &d.n8, &d.levels8, errbuf,
-                                sizeof(errbuf), st);
+    cudaError_t be = build_bvh8(d, (float4 *)(slab + off_bvh8), bvh8_capacity(nt), &d.n8, &d.levels8, &d.root8,
+                                errbuf, sizeof(errbuf), st);
     if (be != cudaSuccess && errbuf[0]) return abort_upload(fail(ctx, RT_ERR_INTERNAL, "%s", errbuf));
     UCK(be, "bvh8");
     d.bvh8 = (const float4 *)(slab + off_bvh8);
@@ -694,7 +694,7 @@ rt_status rtRender(rt_ctx *ctx, rt_scene_id id, const rt_render_params *p, float
     void *scratch = nullptr;
     CK(cudaMallocAsync(&scratch, wavefront_scratch_bytes((uint32_t)pixels), st), "wavefront scratch");
     cudaError_t e = launch_render_wavefront(d, cam, *p, accum, ctx->d_segments, next_counter(ctx), ctx->d_err, scratch,
-                                            topts.sort != 0, st);
+                                            topts.sort != 0, use_wide(topts, d), st);
     cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render launch");
     return RT_SUCCESS;
@@ -770,6 +770,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.wide_minblocks = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.wide_min_tris") {
+    if (value < 0 || value > 0xffffffffll) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.wide_min_tris = (uint32_t)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.wavefront_pixels") {
     if (value < 1 || value > (1ll << 31)) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.wavefront_pixels = (uint64_t)value;
@@ -827,6 +832,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.wide_minblocks") {
     *value = ctx->trace_opts.wide_minblocks;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.wide_min_tris") {
+    *value = ctx->trace_opts.wide_min_tris;
     return RT_SUCCESS;
   }
   if (k == "trace.host_chunk") {
@@ -901,9 +910,11 @@ uint32_t *ctx_err(rt_ctx *ctx) { return ctx->d_err; }
 uint64_t ctx_budget(rt_ctx *ctx) { return ctx->budget; }
 int ctx_device(rt_ctx *ctx) { return ctx->device; }
 cudaStream_t ctx_stream(rt_ctx *ctx) { return ctx->stream; }
-bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort) {
+bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort, bool *wide, uint32_t *min_tris) {
   std::lock_guard<std::mutex> g(ctx->mu);
   if (sort) *sort = ctx->trace_opts.sort != 0;
+  if (wide) *wide = ctx->trace_opts.wide != 0;
+  if (min_tris) *min_tris = ctx->trace_opts.wide_min_tris;
   return use_wavefront(ctx->render_opts, p);
 }
 uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
@@ -929,6 +940,8 @@ struct rt_batch {
   static constexpr int kSides = 4;
   void *wf_scratch[kSides] = {};
   bool wf_sort = true;
+  bool wf_wide = true;
+  uint32_t wf_wide_min = 0;
   uint32_t *counter = nullptr; // [0] tile counter
   cudaStream_t side[kSides] = {}, capture = nullptr;
   cudaEvent_t fork = nullptr, join[kSides] = {};
@@ -989,7 +1002,8 @@ cudaError_t batch_enqueue(rt_ctx *ctx, rt_batch *b, cudaStream_t st) {
       const BatchJob &J = b->wf[j];
       const int k = (int)(j % rt_batch::kSides);
       e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx->d_segments, b->counter + 64 * (1 + k), ctx->d_err,
-                                  b->wf_scratch[k], b->wf_sort, b->side[k], &b->d_wf[j].p.sample_index);
+                                  b->wf_scratch[k], b->wf_sort, b->wf_wide && J.sc.ntris >= b->wf_wide_min,
+                                  b->side[k], &b->d_wf[j].p.sample_index);
     }
     for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaEventRecord(b->join[k], b->side[k]);
   }
@@ -1048,6 +1062,8 @@ rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs,
   b->n = (uint32_t)tiles_jobs.size();
   b->total_tiles = (uint32_t)tiles;
   b->wf_sort = topts.sort != 0;
+  b->wf_wide = topts.wide != 0;
+  b->wf_wide_min = topts.wide_min_tris;
   cudaError_t e = cudaMalloc((void **)&b->d_jobs, sizeof(BatchJob) * std::max(b->n, 1u));
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->counter, 256 * (1 + rt_batch::kSides));
   if (e == cudaSuccess && b->n)

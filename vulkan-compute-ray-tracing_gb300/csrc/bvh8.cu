@@ -11,11 +11,13 @@
 // leaves only, which bounds the node count by (4n - 1) / 7 for n leaves.
 //
 // Layout: a node is 8 slots of 32 bytes (256 bytes, one 256-bit load per
-// slot): (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref, 0). ref >= 0 is a
-// bvh8 node, ~k a leaf (tpre record k, as in bvh2), and an empty slot has
-// every bound +inf, which every slab test misses (entry +inf, or exit -inf
-// for a negative direction component), with ref INT_MIN. Nodes are numbered
-// breadth first, level by level; the children of one node are consecutive.
+// slot): (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref, 0). The filled slots
+// come first. ref >= 0 is an inner child, encoded as (node << 3) | (filled
+// slots of that node - 1) so a traversal loads only the filled slots; ~k is
+// a leaf (tpre record k, as in bvh2). An empty slot has every bound +inf,
+// which every slab test misses (entry +inf, or exit -inf for a negative
+// direction component), and ref INT_MIN. Nodes are numbered breadth first,
+// level by level; the children of one node are consecutive.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -123,14 +125,42 @@ __global__ void k_link8(uint32_t count, uint32_t base, uint32_t next_base, const
   }
 }
 
+// Encodes every inner ref with its child's filled-slot count (all levels
+// are built when this runs).
+__global__ void k_encode8(uint32_t n8, float4 *__restrict__ bvh8, uint32_t *__restrict__ err) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n8) return;
+  float4 *o = bvh8 + 16ull * f;
+  for (int s = 0; s < 8; s++) {
+    float4 w = o[2 * s + 1];
+    const int32_t ref = __float_as_int(w.z);
+    if (ref < 0) continue;
+    if ((uint32_t)ref >= n8) {
+      atomicOr(err, 2u);
+      continue;
+    }
+    const float4 *c = bvh8 + 16ull * ref;
+    int filled = 8;
+    for (int q = 1; q < 8; q++) {
+      if (__float_as_int(c[2 * q + 1].z) == INT_MIN) {
+        filled = q;
+        break;
+      }
+    }
+    w.z = __int_as_float((ref << 3) | (filled - 1));
+    o[2 * s + 1] = w;
+  }
+}
+
 }  // namespace
 
 uint32_t bvh8_capacity(uint32_t ntris) { return ntris ? (uint32_t)((4ull * ntris + 6) / 7 + 1) : 0; }
 
 cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
-                       char *errbuf, size_t errlen, cudaStream_t st) {
+                       int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
   *n8_out = 0;
   *levels_out = 0;
+  *root_out = 7;  // node 0, all slots loaded
   if (d.ntris == 0 || cap == 0 || !bvh8) return cudaErrorInvalidValue;
   if (d.root_ref < 0) {
     // One triangle: a single node with the root leaf in slot 0.
@@ -152,6 +182,7 @@ cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *
     if (e != cudaSuccess) return e;
     *n8_out = 1;
     *levels_out = 1;
+    *root_out = 0;  // node 0, one filled slot
     return cudaSuccess;
   }
   const uint32_t n_pairs = d.ntris - 1;
@@ -191,6 +222,18 @@ cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *
     int32_t *t = fr;
     fr = fr_next;
     fr_next = t;
+  }
+  if (e == cudaSuccess && !bad) {
+    if (base >= (1u << 28)) {
+      bad = 4;
+    } else {
+      k_encode8<<<(base + 255) / 256, 256, 0, st>>>(base, bvh8, errw);
+      e = cudaGetLastError();
+      uint32_t tail = 0;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&tail, errw, 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      bad = tail;
+    }
   }
   cudaFreeAsync(scr, st);
   if (e != cudaSuccess) return e;

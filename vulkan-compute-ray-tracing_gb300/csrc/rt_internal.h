@@ -33,8 +33,9 @@ enum : uint32_t {
 //   leaf_tri  original triangle index of leaf k.
 //   bvh8    the same tree with levels folded into nodes of up to eight
 //           children (bvh8.cu): 8 slots of 32 B, (lo.xyz, hi.x),
-//           (hi.yz, ref, 0), breadth-first numbered, root node 0; leaf refs
-//           are the bvh2 ones (~k). Used by the per-lane 8-wide caster.
+//           (hi.yz, ref, 0), filled slots first, breadth-first numbered,
+//           root node 0; inner refs are (node << 3) | (filled slots - 1),
+//           leaf refs the bvh2 ones (~k). Used by the per-lane 8-wide caster.
 struct DevScene {
   const rt_triangle *tris;
   const rt_material *mats;
@@ -51,6 +52,7 @@ struct DevScene {
   uint32_t depth;
   const float4 *bvh8;
   uint32_t n8, levels8;  // bvh8 nodes and levels (0 when absent)
+  int32_t root8;         // encoded ref of the bvh8 root: (0 << 3) | (filled slots - 1)
 };
 
 // ---------------------------------------------------------------- bvh8.cu
@@ -58,7 +60,7 @@ struct DevScene {
 uint32_t bvh8_capacity(uint32_t ntris);
 // Folds d.bvh2 into bvh8 (capacity `cap` nodes); synchronises `st`.
 cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
-                       char *errbuf, size_t errlen, cudaStream_t st);
+                       int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st);
 
 // ---------------------------------------------------------------- relayout.cu
 // Exclusive scan of n words (in may equal out); `sums` needs ceil(n/1024).
@@ -80,6 +82,7 @@ struct TraceOpts {
   int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
   int wide = 1;     // 1: per-lane chunks are cast over bvh8 with a warp leaf pool (k_trace_wide)
   int wide_minblocks = 6;  // resident 128-thread blocks per SM k_trace_wide is compiled for (8, 6 or 5)
+  uint32_t wide_min_tris = 1u << 17;  // scenes from this many triangles up use the 8-wide caster
   uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
 };
 
@@ -93,6 +96,16 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
                          uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st,
                          const uint32_t *perm = nullptr, uint32_t *chunk_scratch = nullptr);
 size_t trace_chunk_scratch_bytes(uint32_t n);
+// The 8-wide caster over listed 32-ray chunks of a device-sized queue
+// (*d_n rays, at most cap), writing (leaf k, t) hits; wide_ok tells whether
+// the scene's bvh8 can take it.
+bool wide_ok(const DevScene &sc);
+inline bool use_wide(const TraceOpts &o, const DevScene &sc) {
+  return o.wide && sc.ntris >= o.wide_min_tris && wide_ok(sc);
+}
+cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t cap, const uint32_t *d_n,
+                             const uint32_t *perm, const uint32_t *list, const uint32_t *list_count, int2 *hits,
+                             uint32_t *counter, uint32_t *err, int minblocks, cudaStream_t st);
 // Morton bucketing of a ray batch (raysort.cu); `scratch` holds
 // raysort_scratch_bytes(n); *perm_out points into it.
 size_t raysort_scratch_bytes(uint32_t n);
@@ -113,9 +126,12 @@ cudaError_t launch_render(const DevScene &sc, const rt_camera &cam, const rt_ren
 // device word. With d_sample_index the kernels read the first sample index
 // from the device at run time instead of p.sample_index.
 size_t wavefront_scratch_bytes(uint32_t cap);
+// `wide`: bounce rays that fail the packet test are cast by the 8-wide
+// caster (launch_wide_leaf) instead of in place.
 cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
                                     unsigned long long *segments, uint32_t *counter, uint32_t *err, void *scratch,
-                                    bool sort, cudaStream_t st, const uint32_t *d_sample_index = nullptr);
+                                    bool sort, bool wide, cudaStream_t st,
+                                    const uint32_t *d_sample_index = nullptr);
 
 // Render launch-shape knobs (rtSetTuning "render.mode").
 struct RenderOpts {
@@ -174,7 +190,8 @@ cudaStream_t ctx_stream(rt_ctx *ctx);
 // True when rtRender would give a render of these params to the wavefront
 // kernels (render.mode 1, or 2 and >= 2^20 pixels; never the 16-entry
 // compat traversal); *sort receives trace.sort.
-bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort);
+bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort, bool *wide = nullptr,
+                          uint32_t *min_tris = nullptr);
 // Device bytes rtUploadScene allocates for a scene of these counts.
 uint64_t scene_device_bytes(uint32_t n_triangles, uint32_t n_materials, uint32_t n_lights, uint32_t n_spheres);
 

@@ -206,7 +206,8 @@ void scheduler(rt_server *s) {
     std::vector<uint32_t> step(run.size(), 0);
     std::vector<char> lost(run.size(), 0);
     std::vector<BatchJob> wf;
-    bool sort = true;
+    bool sort = true, wide = true;
+    uint32_t wide_min = 0;
     for (size_t i = 0; i < run.size(); i++) {
       SrvReq *q = run[i];
       SrvScene &sc = s->scenes[q->r.scene];
@@ -222,7 +223,7 @@ void scheduler(rt_server *s) {
       B.cam = q->r.camera;
       B.p = rt_render_params{q->r.width, q->r.height, step[i], q->r.max_bounces, q->done_spp, q->r.flags, {0, 0}};
       B.accum = q->d_accum;
-      if (ctx_wavefront_render(s->ctx, B.p, &sort)) {
+      if (ctx_wavefront_render(s->ctx, B.p, &sort, &wide, &wide_min)) {
         wf.push_back(B);
         continue;
       }
@@ -253,7 +254,8 @@ void scheduler(rt_server *s) {
         const int k = (int)(j % rt_server::kSides);
         const BatchJob &J = wf[j];
         e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx_segments(s->ctx), s->d_counter + 64 * (1 + k),
-                                    ctx_err(s->ctx), s->scratch[k], sort, s->side[k]);
+                                    ctx_err(s->ctx), s->scratch[k], sort, wide && J.sc.ntris >= wide_min,
+                                    s->side[k]);
       }
       for (int k = 0; k < sides && e == cudaSuccess; k++) e = cudaEventRecord(s->join[k], s->side[k]);
     }

@@ -313,8 +313,9 @@ constexpr int kPool = 512;       // leaf pool entries per warp (power of two)
 constexpr int kWideRefill = 8;   // idle lanes that trigger a fetch of new rays
 
 // One ray per lane over bvh8 (Ylitie et al., HPG 2017, without the node
-// compression): a step tests all eight child slots of the lane's node (eight
-// independent 256-bit loads), ranks the inner children that are hit by
+// compression): a step tests the filled child slots of the lane's node (up
+// to eight independent 256-bit loads; the count comes with the node's
+// reference), ranks the inner children that are hit by
 // entry distance (pairwise compares), descends into the nearest and pushes
 // the rest onto the lane's stack in near-to-far order. Leaves that are hit
 // go to the warp's FIFO leaf pool in shared memory as (leaf, lane) entries;
@@ -329,9 +330,13 @@ constexpr int kWideRefill = 8;   // idle lanes that trigger a fetch of new rays
 // when it has no node, an empty stack, and the pool has moved past its last
 // entry. Idle lanes claim new rays (slots of the listed chunks, or of the
 // whole batch) once kWideRefill of them are idle.
-template <int STACK, bool REFINE, int MINB>
+// LEAF_OUT: hits are int2 (leaf k, fp32 t) for the wavefront's shading (k =
+// -1 and the ray's tmax when nothing is hit), and the batch size is the
+// device word *d_n (capped at n); otherwise int4 rt_hit records.
+template <int STACK, bool REFINE, int MINB, bool LEAF_OUT>
 __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, const float4 *__restrict__ rays,
-                                                               uint32_t n, int4 *__restrict__ hits,
+                                                               uint32_t n, const uint32_t *d_n,
+                                                               void *__restrict__ hits_out,
                                                                uint32_t *__restrict__ counter, uint32_t *err,
                                                                const uint32_t *__restrict__ perm,
                                                                const uint32_t *__restrict__ list,
@@ -350,6 +355,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
   float4 *hit_s = s_hit[warp];
   uint32_t *pool = s_pool[warp];
   const float INF = __int_as_float(0x7f800000);
+  if (d_n) n = min(n, *d_n);
   const uint32_t total = list ? min(*list_count, (n + 31) / 32) * 32u : n;
   const float4 *__restrict__ bvh8 = sc.bvh8;
   const int n8 = (int)sc.n8, ntris = (int)sc.ntris;
@@ -366,15 +372,21 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
     if (ray_i >= 0 && node < 0 && sp == 0 && (int)(head - mlp1) >= 0) {
       const unsigned long long key = key_v[lane];
       const float tmax = ray_s[lane][1].w;
-      int4 h = make_int4(-1, 0, 0, 0);
-      if ((uint32_t)(key >> 32) != ord_f(__fadd_rn(tmax, 0.0f))) {
-        const int tri = (int)(uint32_t)key;
-        const float4 w = hit_s[lane];
-        float t = w.x, u = w.y, v = w.z;
-        if (REFINE) refine_fp64(sc.tris, tri, r.o, r.d, t, u, v);
-        h = make_int4(tri, __float_as_int(t), __float_as_int(u), __float_as_int(v));
+      const bool got = (uint32_t)(key >> 32) != ord_f(__fadd_rn(tmax, 0.0f));
+      const float4 w = hit_s[lane];
+      if (LEAF_OUT) {
+        static_cast<int2 *>(hits_out)[ray_i] =
+            got ? make_int2(__float_as_int(w.w), __float_as_int(w.x)) : make_int2(-1, __float_as_int(tmax));
+      } else {
+        int4 h = make_int4(-1, 0, 0, 0);
+        if (got) {
+          const int tri = (int)(uint32_t)key;
+          float t = w.x, u = w.y, v = w.z;
+          if (REFINE) refine_fp64(sc.tris, tri, r.o, r.d, t, u, v);
+          h = make_int4(tri, __float_as_int(t), __float_as_int(u), __float_as_int(v));
+        }
+        static_cast<int4 *>(hits_out)[ray_i] = h;
       }
-      hits[ray_i] = h;
       ray_i = -1;
     }
     // Idle lanes claim new rays.
@@ -402,7 +414,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
             mlp1 = head;
             const float root = slab_enter(r, sc.root_lo[0], sc.root_hi[0], sc.root_lo[1], sc.root_hi[1],
                                           sc.root_lo[2], sc.root_hi[2], r1.w);
-            node = root < INF ? 0 : -1;
+            node = root < INF ? sc.root8 : -1;
           }
         }
       }
@@ -414,17 +426,22 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
     uint32_t leafmask = 0;
     if (ray_i >= 0 && node >= 0) {
       const float closest = ord_inv((uint32_t)(key_v[lane] >> 32));
-      const float4 *N = bvh8 + 16ll * node;
+      const float4 *N = bvh8 + 16ll * (node >> 3);
+      const int filled = (node & 7) + 1;
       uint32_t key[8];
 #pragma unroll
       for (int s = 0; s < 8; s++) {
-        float4 a, b;
-        load_slot8(N + 2 * s, a, b);
-        ref[s] = __float_as_int(b.z);
-        const float t = slab_enter(r, a.x, a.w, a.y, b.x, a.z, b.y, closest);
-        const bool hit = t < INF;
-        key[s] = (hit && ref[s] >= 0) ? ((__float_as_uint(t) & ~7u) | (uint32_t)s) : 0xffffffffu;
-        if (hit && ref[s] < 0) leafmask |= 1u << s;
+        key[s] = 0xffffffffu;
+        ref[s] = INT_MIN;
+        if (s < filled) {
+          float4 a, b;
+          load_slot8(N + 2 * s, a, b);
+          ref[s] = __float_as_int(b.z);
+          const float t = slab_enter(r, a.x, a.w, a.y, b.x, a.z, b.y, closest);
+          const bool hit = t < INF;
+          if (hit && ref[s] >= 0) key[s] = (__float_as_uint(t) & ~7u) | (uint32_t)s;
+          if (hit && ref[s] < 0) leafmask |= 1u << s;
+        }
       }
       int rk[8];
       int cnt = 0;
@@ -456,15 +473,15 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
         sp += cnt > 0 ? cnt - 1 : 0;
       }
       node = next;
-      if (node >= n8 || ++steps > step_cap) {
-        atomicOr(err, node >= n8 ? KERR_BAD_INDEX : KERR_TIMEOUT);
+      if ((node >> 3) >= n8 || ++steps > step_cap) {
+        atomicOr(err, (node >> 3) >= n8 ? KERR_BAD_INDEX : KERR_TIMEOUT);
         node = -1;
         sp = 0;
       }
     }
     if (ray_i >= 0 && node < 0 && sp > 0) {
       node = stack[--sp];
-      if (node < 0 || node >= n8) {
+      if (node < 0 || (node >> 3) >= n8) {
         atomicOr(err, KERR_BAD_INDEX);
         node = -1;
         sp = 0;
@@ -506,11 +523,12 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
       bool acc = false;
       unsigned long long cand = 0;
       uint32_t owner = 0;
+      int k = 0;
       float ct = 0.0f, cu = 0.0f, cv = 0.0f;
       if (lane < cnt) {
         const uint32_t e = pool[(head + lane) & (kPool - 1)];
         owner = e & 31u;
-        const int k = (int)(e >> 5);
+        k = (int)(e >> 5);
         const float4 q0 = ray_s[owner][0], q1 = ray_s[owner][1];
         const unsigned long long cur = key_v[owner];
         if (tri_candidate(sc.tpre, k, mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), q0.w,
@@ -525,7 +543,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
         }
       }
       __syncwarp();
-      if (acc && key_v[owner] == cand) hit_s[owner] = make_float4(ct, cu, cv, 0.0f);
+      if (acc && key_v[owner] == cand) hit_s[owner] = make_float4(ct, cu, cv, __int_as_float(k));
       __syncwarp();
       head += cnt;
     }
@@ -570,10 +588,11 @@ template <int STACK, bool REFINE>
 cudaError_t launch_wide(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
                         uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
                         int minblocks, cudaStream_t st) {
-  auto kern = minblocks >= 8 ? k_trace_wide<STACK, REFINE, 8>
-              : minblocks >= 6 ? k_trace_wide<STACK, REFINE, 6>
-                               : k_trace_wide<STACK, REFINE, 5>;
-  kern<<<persistent_grid(kern, n), kTraceBlock, 0, st>>>(sc, rays, n, hits, counter, err, perm, list, list_count);
+  auto kern = minblocks >= 8 ? k_trace_wide<STACK, REFINE, 8, false>
+              : minblocks >= 6 ? k_trace_wide<STACK, REFINE, 6, false>
+                               : k_trace_wide<STACK, REFINE, 5, false>;
+  kern<<<persistent_grid(kern, n), kTraceBlock, 0, st>>>(sc, rays, n, nullptr, hits, counter, err, perm, list,
+                                                          list_count);
   return cudaGetLastError();
 }
 
@@ -600,7 +619,7 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
       list_count = chunk_scratch;
       lane_counter = chunk_scratch + 1;
     }
-    if (opts.wide && sc.bvh8 && sc.levels8 >= 1 && sc.ntris < (1u << 27)) {
+    if (use_wide(opts, sc)) {
       // The stack holds at most 7 entries per level above the last.
       const uint32_t need = 7u * (sc.levels8 - 1);
       if (need <= 64)
@@ -622,6 +641,30 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
 }
 
 }  // namespace
+
+bool wide_ok(const DevScene &sc) {
+  return sc.bvh8 && sc.levels8 >= 1 && sc.ntris < (1u << 27) && 7u * (sc.levels8 - 1) <= 128u;
+}
+
+cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t cap, const uint32_t *d_n,
+                             const uint32_t *perm, const uint32_t *list, const uint32_t *list_count, int2 *hits,
+                             uint32_t *counter, uint32_t *err, int minblocks, cudaStream_t st) {
+  if (!wide_ok(sc)) return cudaErrorInvalidValue;
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const float4 *r4 = reinterpret_cast<const float4 *>(rays);
+  auto go = [&](auto kern) {
+    kern<<<persistent_grid(kern, cap), kTraceBlock, 0, st>>>(sc, r4, cap, d_n, hits, counter, err, perm, list,
+                                                              list_count);
+    return cudaGetLastError();
+  };
+  if (7u * (sc.levels8 - 1) <= 64u)
+    return minblocks >= 8 ? go(k_trace_wide<64, false, 8, true>) : go(k_trace_wide<64, false, 6, true>);
+  return minblocks >= 8 ? go(k_trace_wide<128, false, 8, true>) : go(k_trace_wide<128, false, 6, true>);
+}
 
 size_t trace_chunk_scratch_bytes(uint32_t n) { return 4ull * (64 + (n + 31) / 32); }
 

@@ -34,7 +34,8 @@ struct WfBufs {
   int2 *cam_hits;  // bounce-0 hits of the call's first sample, reused by the others
   float4 *color;
   uint32_t *rng;
-  uint32_t *counts;  // [0], [1]: queue lengths
+  uint32_t *counts;  // [0], [1]: queue lengths; [2] listed chunks, [3] wide-caster counter
+  uint32_t *list;    // chunks of the queue left to the 8-wide caster
   void *sort;
 };
 
@@ -59,6 +60,8 @@ WfBufs carve(void *scratch, uint32_t cap) {
   p += a256(4ull * cap);
   b.counts = reinterpret_cast<uint32_t *>(p);
   p += 256;
+  b.list = reinterpret_cast<uint32_t *>(p);
+  p += a256(4ull * ((cap + 31) / 32));
   b.sort = p;
   return b;
 }
@@ -83,14 +86,16 @@ __global__ void k_wf_raygen(rt_camera cam, uint32_t W, uint32_t H, uint32_t s, c
 
 // Closest triangle per queued ray. A warp whose 32 rays are coherent (the
 // camera rays of bounce 0 in pixel order, or any bundle sharing an origin)
-// traverses them as one packet; other warps run each lane's ray with
-// postponed leaves. Both return every ray's own closest hit.
+// traverses them as one packet; other warps list their chunk for the 8-wide
+// caster (list != NULL) or run each lane's ray with postponed leaves. All
+// return every ray's own closest hit.
 template <int STACK>
 __global__ void __launch_bounds__(kWfBlock, 12) k_wf_extend(DevScene sc, const float4 *__restrict__ rays,
                                                             uint32_t cap, const uint32_t *count,
                                                             const uint32_t *__restrict__ perm,
                                                             int2 *__restrict__ hits, uint32_t *counter,
-                                                            uint32_t *err) {
+                                                            uint32_t *err, uint32_t *__restrict__ list,
+                                                            uint32_t *__restrict__ list_count) {
   __shared__ int s_stack[kWfBlock / 32][STACK];
   const uint32_t n = min(cap, *count);
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -119,6 +124,9 @@ __global__ void __launch_bounds__(kWfBlock, 12) k_wf_extend(DevScene sc, const f
 #define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, u, v, s_stack[warp], err)
       RTGB_OCT_DISPATCH(oct, RTGB_CALL)
 #undef RTGB_CALL
+    } else if (list) {
+      if (lane == 0) list[atomicAdd(list_count, 1u)] = base;
+      continue;
     } else {
 #define RTGB_CALL(O) k = traverse_spec<STACK, O>(sc, r, active, closest, u, v, err)
       RTGB_OCT_DISPATCH(oct, RTGB_CALL)
@@ -205,14 +213,15 @@ int g_sms = 0;
 
 size_t wavefront_scratch_bytes(uint32_t cap) {
   return 2 * (a256(sizeof(rt_ray) * (size_t)cap) + a256(4ull * cap)) + 2 * a256(8ull * cap) + a256(16ull * cap) +
-         a256(4ull * cap) + 256 + a256(raysort_scratch_bytes(cap));
+         a256(4ull * cap) + 256 + a256(4ull * ((cap + 31) / 32)) + a256(raysort_scratch_bytes(cap));
 }
 
 cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, const rt_render_params &p, float *accum,
                                     unsigned long long *segments, uint32_t *counter, uint32_t *err, void *scratch,
-                                    bool sort, cudaStream_t st, const uint32_t *d_sample_index) {
+                                    bool sort, bool wide, cudaStream_t st, const uint32_t *d_sample_index) {
   const uint32_t W = p.width, H = p.height, cap = W * H;
   if (cap == 0 || p.spp == 0) return cudaSuccess;
+  const bool use_wide = wide && wide_ok(sc);
   if (g_sms == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -247,10 +256,18 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
       if (sort && (e = launch_raysort(b.rays[in], cap, b.counts + in, b.sort, &perm, st)) != cudaSuccess) return e;
       if ((e = cudaMemsetAsync(counter, 0, 4, st)) != cudaSuccess) return e;
       const float4 *r4 = reinterpret_cast<const float4 *>(b.rays[in]);
+      uint32_t *list = use_wide ? b.list : nullptr;
+      if (use_wide && (e = cudaMemsetAsync(b.counts + 2, 0, 8, st)) != cudaSuccess) return e;
       if (sc.depth <= 32)
-        k_wf_extend<32><<<egrid, kWfBlock, 0, st>>>(sc, r4, cap, b.counts + in, perm, b.hits, counter, err);
+        k_wf_extend<32><<<egrid, kWfBlock, 0, st>>>(sc, r4, cap, b.counts + in, perm, b.hits, counter, err, list,
+                                                    b.counts + 2);
       else
-        k_wf_extend<64><<<egrid, kWfBlock, 0, st>>>(sc, r4, cap, b.counts + in, perm, b.hits, counter, err);
+        k_wf_extend<64><<<egrid, kWfBlock, 0, st>>>(sc, r4, cap, b.counts + in, perm, b.hits, counter, err, list,
+                                                    b.counts + 2);
+      if (use_wide &&
+          (e = launch_wide_leaf(sc, b.rays[in], cap, b.counts + in, perm, b.list, b.counts + 2, b.hits,
+                                b.counts + 3, err, 6, st)) != cudaSuccess)
+        return e;
       if (bounce == 0 && p.spp > 1 &&
           (e = cudaMemcpyAsync(b.cam_hits, b.hits, 8ull * cap, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
         return e;
