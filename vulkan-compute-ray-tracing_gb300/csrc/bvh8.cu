@@ -126,15 +126,20 @@ __global__ void k_link8(uint32_t count, uint32_t base, uint32_t next_base, const
 }
 
 // Encodes every inner ref with its child's filled-slot count (all levels
-// are built when this runs).
-__global__ void k_encode8(uint32_t n8, float4 *__restrict__ bvh8, uint32_t *__restrict__ err) {
+// are built when this runs), and range-checks every leaf ref, which the
+// traversal then uses without a check.
+__global__ void k_encode8(uint32_t n8, uint32_t ntris, float4 *__restrict__ bvh8, uint32_t *__restrict__ err) {
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= n8) return;
   float4 *o = bvh8 + 16ull * f;
   for (int s = 0; s < 8; s++) {
     float4 w = o[2 * s + 1];
     const int32_t ref = __float_as_int(w.z);
-    if (ref < 0) continue;
+    if (ref == INT_MIN) continue;
+    if (ref < 0) {
+      if ((uint32_t)~ref >= ntris) atomicOr(err, 2u);
+      continue;
+    }
     if ((uint32_t)ref >= n8) {
       atomicOr(err, 2u);
       continue;
@@ -227,7 +232,7 @@ cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *
     if (base >= (1u << 28)) {
       bad = 4;
     } else {
-      k_encode8<<<(base + 255) / 256, 256, 0, st>>>(base, bvh8, errw);
+      k_encode8<<<(base + 255) / 256, 256, 0, st>>>(base, d.ntris, bvh8, errw);
       e = cudaGetLastError();
       uint32_t tail = 0;
       if (e == cudaSuccess) e = cudaMemcpyAsync(&tail, errw, 4, cudaMemcpyDeviceToHost, st);

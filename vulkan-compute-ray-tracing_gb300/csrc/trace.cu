@@ -345,6 +345,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
   __shared__ unsigned long long s_key[kTraceBlock / 32][32];
   __shared__ float4 s_hit[kTraceBlock / 32][32];
   __shared__ uint32_t s_pool[kTraceBlock / 32][kPool];
+  __shared__ int s_ref[kTraceBlock / 32][8][32];  // child refs of the lane's node, lane-major
   uint32_t lane;
   asm("mov.u32 %0, %%laneid;" : "=r"(lane));
   const uint32_t warp = threadIdx.x >> 5;
@@ -354,11 +355,12 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
   unsigned long long *key_a = s_key[warp];
   float4 *hit_s = s_hit[warp];
   uint32_t *pool = s_pool[warp];
+  int(*ref_s)[32] = s_ref[warp];
   const float INF = __int_as_float(0x7f800000);
   if (d_n) n = min(n, *d_n);
   const uint32_t total = list ? min(*list_count, (n + 31) / 32) * 32u : n;
   const float4 *__restrict__ bvh8 = sc.bvh8;
-  const int n8 = (int)sc.n8, ntris = (int)sc.ntris;
+  const int n8 = (int)sc.n8;
   const uint32_t step_cap = sc.n8 + 16u;
 
   int stack[STACK];
@@ -443,34 +445,38 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
           if (hit && ref[s] < 0) leafmask |= 1u << s;
         }
       }
-      int rk[8];
+      // Near-to-far order: sort the slot-tagged keys (Batcher's 19-comparator
+      // network for 8), then read each child's ref back by slot from the
+      // lane's own column of s_ref.
       int cnt = 0;
 #pragma unroll
       for (int s = 0; s < 8; s++) {
-        rk[s] = 0;
         cnt += key[s] != 0xffffffffu ? 1 : 0;
+        ref_s[s][lane] = ref[s];
       }
-#pragma unroll
-      for (int s = 1; s < 8; s++) {
-#pragma unroll
-        for (int q = 0; q < s; q++) {
-          const bool lt = key[q] < key[s];
-          rk[s] += lt ? 1 : 0;
-          rk[q] += lt ? 0 : 1;
-        }
-      }
+#define RTGB_CAS(i, j)                                    \
+  {                                                       \
+    const uint32_t lo_ = min(key[i], key[j]), hi_ = max(key[i], key[j]); \
+    key[i] = lo_;                                         \
+    key[j] = hi_;                                         \
+  }
+      RTGB_CAS(0, 1) RTGB_CAS(2, 3) RTGB_CAS(4, 5) RTGB_CAS(6, 7)
+      RTGB_CAS(0, 2) RTGB_CAS(1, 3) RTGB_CAS(4, 6) RTGB_CAS(5, 7)
+      RTGB_CAS(1, 2) RTGB_CAS(5, 6)
+      RTGB_CAS(0, 4) RTGB_CAS(1, 5) RTGB_CAS(2, 6) RTGB_CAS(3, 7)
+      RTGB_CAS(2, 4) RTGB_CAS(3, 5)
+      RTGB_CAS(1, 2) RTGB_CAS(3, 4) RTGB_CAS(5, 6)
+#undef RTGB_CAS
       int next = -1;
       if (cnt > 0 && sp + cnt - 1 > STACK) {
         atomicOr(err, KERR_STACK_OVERFLOW);
         sp = 0;
-      } else {
+      } else if (cnt > 0) {
+        next = ref_s[key[0] & 7u][lane];
 #pragma unroll
-        for (int s = 0; s < 8; s++) {
-          if (key[s] == 0xffffffffu) continue;
-          if (rk[s] == 0) next = ref[s];
-          else stack[sp + cnt - 1 - rk[s]] = ref[s];
-        }
-        sp += cnt > 0 ? cnt - 1 : 0;
+        for (int i = 1; i < 8; i++)
+          if (i < cnt) stack[sp + cnt - 1 - i] = ref_s[key[i] & 7u][lane];
+        sp += cnt - 1;
       }
       node = next;
       if ((node >> 3) >= n8 || ++steps > step_cap) {
@@ -502,12 +508,8 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
 #pragma unroll
       for (int s = 0; s < 8; s++) {
         if (!((leafmask >> s) & 1u)) continue;
-        int k = ~ref[s];
-        if (k >= ntris) {
-          atomicOr(err, KERR_BAD_INDEX);
-          k = 0;
-        }
-        pool[pos & (kPool - 1)] = ((uint32_t)k << 5) | lane;
+        // Leaf refs were range-checked when the bvh8 was built (k_encode8).
+        pool[pos & (kPool - 1)] = ((uint32_t)~ref[s] << 5) | lane;
         pos++;
       }
       mlp1 = pos;
