@@ -302,6 +302,13 @@ def test_alt_tree_mode_same_hits(rt, orc, ctx, builder):
         ties = (st[:, 2] & 1) != 0
         compare(gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32), want, ties)
         compare(gpu_trace(ctx, ref_sc, rays, flags=rt.HIT_FP32), want, ties)
+        # The 8-wide fold of this tree (forced below its size threshold).
+        old_min = ctx.get_tuning("trace.wide_min_tris")
+        ctx.set_tuning("trace.wide_min_tris", 0)
+        try:
+            compare(gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32), want, ties)
+        finally:
+            ctx.set_tuning("trace.wide_min_tris", old_min)
     finally:
         sc.release()
         ref_sc.release()
