@@ -775,6 +775,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.wide_min_tris = (uint32_t)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.wide_refill") {
+    if (value < 1 || value > 32) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.wide_refill = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.wavefront_pixels") {
     if (value < 1 || value > (1ll << 31)) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.wavefront_pixels = (uint64_t)value;
@@ -836,6 +841,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.wide_min_tris") {
     *value = ctx->trace_opts.wide_min_tris;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.wide_refill") {
+    *value = ctx->trace_opts.wide_refill;
     return RT_SUCCESS;
   }
   if (k == "trace.host_chunk") {

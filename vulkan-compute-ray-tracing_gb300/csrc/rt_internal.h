@@ -82,6 +82,7 @@ struct TraceOpts {
   int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
   int wide = 1;     // 1: per-lane chunks are cast over bvh8 with a warp leaf pool (k_trace_wide)
   int wide_minblocks = 6;  // resident 128-thread blocks per SM k_trace_wide is compiled for (8, 6 or 5)
+  int wide_refill = 4;     // idle lanes of a k_trace_wide warp that trigger a fetch of new rays (1..32)
   uint32_t wide_min_tris = 1u << 17;  // scenes from this many triangles up use the 8-wide caster
   uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
 };
@@ -105,7 +106,7 @@ inline bool use_wide(const TraceOpts &o, const DevScene &sc) {
 }
 cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t cap, const uint32_t *d_n,
                              const uint32_t *perm, const uint32_t *list, const uint32_t *list_count, int2 *hits,
-                             uint32_t *counter, uint32_t *err, int minblocks, cudaStream_t st);
+                             uint32_t *counter, uint32_t *err, int minblocks, int refill, cudaStream_t st);
 // Morton bucketing of a ray batch (raysort.cu); `scratch` holds
 // raysort_scratch_bytes(n); *perm_out points into it.
 size_t raysort_scratch_bytes(uint32_t n);

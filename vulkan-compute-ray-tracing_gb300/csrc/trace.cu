@@ -310,7 +310,6 @@ __device__ __forceinline__ bool tri_candidate(const float4 *__restrict__ tpre, i
 }
 
 constexpr int kPool = 512;       // leaf pool entries per warp (power of two)
-constexpr int kWideRefill = 8;   // idle lanes that trigger a fetch of new rays
 
 // One ray per lane over bvh8 (Ylitie et al., HPG 2017, without the node
 // compression): a step tests the filled child slots of the lane's node (up
@@ -329,7 +328,7 @@ constexpr int kWideRefill = 8;   // idle lanes that trigger a fetch of new rays
 // leaves are tested. The winner of a round stores its t, u, v. A ray is done
 // when it has no node, an empty stack, and the pool has moved past its last
 // entry. Idle lanes claim new rays (slots of the listed chunks, or of the
-// whole batch) once kWideRefill of them are idle.
+// whole batch) once `refill` of them are idle.
 // LEAF_OUT: hits are int2 (leaf k, fp32 t) for the wavefront's shading (k =
 // -1 and the ray's tmax when nothing is hit), and the batch size is the
 // device word *d_n (capped at n); otherwise int4 rt_hit records.
@@ -340,7 +339,8 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
                                                                uint32_t *__restrict__ counter, uint32_t *err,
                                                                const uint32_t *__restrict__ perm,
                                                                const uint32_t *__restrict__ list,
-                                                               const uint32_t *__restrict__ list_count) {
+                                                               const uint32_t *__restrict__ list_count,
+                                                               int refill) {
   __shared__ float4 s_ray[kTraceBlock / 32][32][2];
   __shared__ unsigned long long s_key[kTraceBlock / 32][32];
   __shared__ float4 s_hit[kTraceBlock / 32][32];
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
     }
     // Idle lanes claim new rays.
     const uint32_t idle = __ballot_sync(0xffffffffu, ray_i < 0);
-    if (!exhausted && __popc(idle) >= kWideRefill) {
+    if (!exhausted && __popc(idle) >= refill) {
       const uint32_t cnt = __popc(idle), leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(counter, cnt);
@@ -589,12 +589,12 @@ cudaError_t launch_lanes(const DevScene &sc, const float4 *rays, uint32_t n, int
 template <int STACK, bool REFINE>
 cudaError_t launch_wide(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
                         uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
-                        int minblocks, cudaStream_t st) {
+                        int minblocks, int refill, cudaStream_t st) {
   auto kern = minblocks >= 8 ? k_trace_wide<STACK, REFINE, 8, false>
               : minblocks >= 6 ? k_trace_wide<STACK, REFINE, 6, false>
                                : k_trace_wide<STACK, REFINE, 5, false>;
   kern<<<persistent_grid(kern, n), kTraceBlock, 0, st>>>(sc, rays, n, nullptr, hits, counter, err, perm, list,
-                                                          list_count);
+                                                          list_count, refill);
   return cudaGetLastError();
 }
 
@@ -626,10 +626,10 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
       const uint32_t need = 7u * (sc.levels8 - 1);
       if (need <= 64)
         return launch_wide<64, REFINE>(sc, r4, n, h4, lane_counter, err, perm, list, list_count,
-                                       opts.wide_minblocks, st);
+                                       opts.wide_minblocks, opts.wide_refill, st);
       if (need <= 128)
         return launch_wide<128, REFINE>(sc, r4, n, h4, lane_counter, err, perm, list, list_count,
-                                        opts.wide_minblocks, st);
+                                        opts.wide_minblocks, opts.wide_refill, st);
     }
     if (opts.minblocks >= 16)
       return launch_lanes<STACK, REFINE, 16>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec, st);
@@ -650,7 +650,7 @@ bool wide_ok(const DevScene &sc) {
 
 cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t cap, const uint32_t *d_n,
                              const uint32_t *perm, const uint32_t *list, const uint32_t *list_count, int2 *hits,
-                             uint32_t *counter, uint32_t *err, int minblocks, cudaStream_t st) {
+                             uint32_t *counter, uint32_t *err, int minblocks, int refill, cudaStream_t st) {
   if (!wide_ok(sc)) return cudaErrorInvalidValue;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -660,7 +660,7 @@ cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t ca
   const float4 *r4 = reinterpret_cast<const float4 *>(rays);
   auto go = [&](auto kern) {
     kern<<<persistent_grid(kern, cap), kTraceBlock, 0, st>>>(sc, r4, cap, d_n, hits, counter, err, perm, list,
-                                                              list_count);
+                                                              list_count, refill);
     return cudaGetLastError();
   };
   if (7u * (sc.levels8 - 1) <= 64u)

@@ -266,7 +266,7 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
                                                     b.counts + 2);
       if (use_wide &&
           (e = launch_wide_leaf(sc, b.rays[in], cap, b.counts + in, perm, b.list, b.counts + 2, b.hits,
-                                b.counts + 3, err, 6, st)) != cudaSuccess)
+                                b.counts + 3, err, 6, 4, st)) != cudaSuccess)
         return e;
       if (bounce == 0 && p.spp > 1 &&
           (e = cudaMemcpyAsync(b.cam_hits, b.hits, 8ull * cap, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
