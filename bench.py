@@ -165,9 +165,9 @@ def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 30.0):
     oracle.trace(tris, nodes, b, slack=0.0)
     dt = time.perf_counter() - t0
     n = len(a) + len(b)
+    which = "every ray of both batches" if stride == 1 else f"one ray in {stride} of each batch"
     return {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": thr, "kind": "port",
-            "sample": f"one ray in {stride} of each batch ({n} rays), oracle fp32 culled traversal, "
-                      f"{thr} OpenMP threads, {dt:.1f} s"}
+            "sample": f"{which} ({n} rays), oracle fp32 culled traversal, {thr} OpenMP threads, {dt:.1f} s"}
 
 
 def run_reference(args):
