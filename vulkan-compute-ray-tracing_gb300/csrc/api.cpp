@@ -152,7 +152,7 @@ SlabLayout slab_layout(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
   L.tpre = L.bvh2 + align256(64ull * ninner);
   L.leaf = L.tpre + align256(48ull * nt);
   L.bvh8 = L.leaf + align256(4ull * nt);
-  L.total = L.bvh8 + align256(256ull * bvh8_capacity(nt));
+  L.total = L.bvh8 + align256(kBvh8NodeBytes * bvh8_capacity(nt));
   return L;
 }
 
@@ -471,8 +471,8 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   // The 8-wide fold of the same tree.
   {
     char errbuf[128] = {0};
-    cudaError_t be = build_bvh8(d, (float4 *)(slab + off_bvh8), bvh8_capacity(nt), &d.n8, &d.levels8, &d.root8,
-                                errbuf, sizeof(errbuf), st);
+    cudaError_t be = build_bvh8(d, slab + off_bvh8, bvh8_capacity(nt), &d.n8, &d.levels8, &d.root8, errbuf,
+                                sizeof(errbuf), st);
     if (be != cudaSuccess && errbuf[0]) return abort_upload(fail(ctx, RT_ERR_INTERNAL, "%s", errbuf));
     UCK(be, "bvh8");
     d.bvh8 = (const float4 *)(slab + off_bvh8);

@@ -10,14 +10,22 @@
 // BVHs", HPG 2017). A node with fewer than eight children therefore holds
 // leaves only, which bounds the node count by (4n - 1) / 7 for n leaves.
 //
-// Layout: a node is 8 slots of 32 bytes (256 bytes, one 256-bit load per
-// slot): (lo.x, lo.y, lo.z, hi.x), (hi.y, hi.z, ref, 0). The filled slots
-// come first. ref >= 0 is an inner child, encoded as (node << 3) | (filled
-// slots of that node - 1) so a traversal loads only the filled slots; ~k is
-// a leaf (tpre record k, as in bvh2). An empty slot has every bound +inf,
-// which every slab test misses (entry +inf, or exit -inf for a negative
-// direction component), and ref INT_MIN. Nodes are numbered breadth first,
-// level by level; the children of one node are consecutive.
+// The fold is built in fp32 (8 slots of 32 bytes: (lo.x, lo.y, lo.z, hi.x),
+// (hi.y, hi.z, ref, 0), filled slots first, empty slots ref INT_MIN) and
+// then stored quantized, 96 bytes per node (k_quantize8, the compression of
+// Ylitie et al. with explicit child refs):
+//   words 0-2    origin o: the lo corner of the union of the children
+//   word 3       int8 exponents ex, ey, ez; filled-slot count
+//   words 4-15   8-bit child bounds qlo.x[8], qlo.y, qlo.z, qhi.x, qhi.y,
+//                qhi.z (slot s in byte s & 3 of word 2 * plane + (s >> 2))
+//   words 16-23  child refs
+// A child's box decodes to o + q * 2^e per axis. qlo is rounded down and
+// qhi up, and both are checked against the fp32 box, so the decoded box
+// always contains the original one. Refs: >= 0 is an inner child, encoded
+// as (node << 3) | (filled slots of that node - 1) so a traversal decodes
+// only the filled slots; ~k is a leaf (tpre record k, as in bvh2). Nodes
+// are numbered breadth first, level by level; the children of one node are
+// consecutive.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -157,15 +165,73 @@ __global__ void k_encode8(uint32_t n8, uint32_t ntris, float4 *__restrict__ bvh8
   }
 }
 
+// fp32 fold -> 96-byte quantized nodes.
+__global__ void k_quantize8(const float4 *__restrict__ wide, uint32_t n8, uint4 *__restrict__ out,
+                            uint32_t *__restrict__ err) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n8) return;
+  const float4 *W = wide + 16ull * f;
+  float lo[8][3], hi[8][3];
+  int32_t ref[8];
+  int filled = 0;
+  for (int s = 0; s < 8; s++) {
+    const float4 a = W[2 * s], b = W[2 * s + 1];
+    lo[s][0] = a.x, lo[s][1] = a.y, lo[s][2] = a.z;
+    hi[s][0] = a.w, hi[s][1] = b.x, hi[s][2] = b.y;
+    ref[s] = __float_as_int(b.z);
+    if (ref[s] != INT_MIN) filled = s + 1;
+  }
+  uint32_t w[24];
+  for (int i = 0; i < 24; i++) w[i] = 0;
+  uint32_t ebytes = (uint32_t)filled << 24;
+  for (int k = 0; k < 3; k++) {
+    float ulo = lo[0][k], uhi = hi[0][k];
+    for (int s = 1; s < filled; s++) {
+      ulo = fminf(ulo, lo[s][k]);
+      uhi = fmaxf(uhi, hi[s][k]);
+    }
+    const double E = (double)uhi - (double)ulo;
+    int e = -126;
+    if (E > 0.0) {
+      int e0 = 0;
+      frexp(E / 255.0, &e0);  // E / 255 <= 2^e0
+      e = (E <= 255.0 * ldexp(1.0, e0 - 1)) ? e0 - 1 : e0;
+      e = e < -126 ? -126 : (e > 127 ? 127 : e);
+    }
+    const double sc = ldexp(1.0, e);
+    if (E > 255.0 * sc) atomicOr(err, 8u);
+    for (int s = 0; s < filled; s++) {
+      int ql = (int)floor(((double)lo[s][k] - (double)ulo) / sc);
+      ql = ql < 0 ? 0 : (ql > 255 ? 255 : ql);
+      while (ql > 0 && (double)ulo + ql * sc > (double)lo[s][k]) ql--;
+      int qh = (int)ceil(((double)hi[s][k] - (double)ulo) / sc);
+      qh = qh < 0 ? 0 : (qh > 255 ? 255 : qh);
+      while (qh < 255 && (double)ulo + qh * sc < (double)hi[s][k]) qh++;
+      if ((double)ulo + ql * sc > (double)lo[s][k] || (double)ulo + qh * sc < (double)hi[s][k]) atomicOr(err, 8u);
+      w[4 + 2 * k + (s >> 2)] |= (uint32_t)ql << (8 * (s & 3));
+      w[10 + 2 * k + (s >> 2)] |= (uint32_t)qh << (8 * (s & 3));
+    }
+    w[k] = __float_as_uint(ulo);
+    ebytes |= ((uint32_t)(e & 0xff)) << (8 * k);
+  }
+  w[3] = ebytes;
+  for (int s = 0; s < 8; s++) w[16 + s] = (uint32_t)ref[s];
+  uint4 *o = out + 6ull * f;
+  for (int i = 0; i < 6; i++) o[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+}
+
 }  // namespace
 
 uint32_t bvh8_capacity(uint32_t ntris) { return ntris ? (uint32_t)((4ull * ntris + 6) / 7 + 1) : 0; }
 
-cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
-                       int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
+namespace {
+
+// The fp32 fold (256-byte nodes) into `bvh8`, which holds `cap` nodes.
+cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
+                            int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
   *n8_out = 0;
   *levels_out = 0;
-  *root_out = 7;  // node 0, all slots loaded
+  *root_out = 7;  // node 0, all slots decoded
   if (d.ntris == 0 || cap == 0 || !bvh8) return cudaErrorInvalidValue;
   if (d.root_ref < 0) {
     // One triangle: a single node with the root leaf in slot 0.
@@ -247,6 +313,38 @@ cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *
     return cudaErrorInvalidValue;
   }
   *n8_out = base;
+  *levels_out = levels;
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
+                       int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
+  *n8_out = 0;
+  *levels_out = 0;
+  if (d.ntris == 0 || cap == 0 || !bvh8q) return cudaErrorInvalidValue;
+  float4 *wide = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&wide, 256ull * cap + 256, st);
+  if (e != cudaSuccess) return e;
+  uint32_t *errw = reinterpret_cast<uint32_t *>(wide + 16ull * cap);
+  uint32_t n8 = 0, levels = 0;
+  e = build_wide_fp32(d, wide, cap, &n8, &levels, root_out, errbuf, errlen, st);
+  uint32_t bad = 0;
+  if (e == cudaSuccess) e = cudaMemsetAsync(errw, 0, 4, st);
+  if (e == cudaSuccess) {
+    k_quantize8<<<(n8 + 127) / 128, 128, 0, st>>>(wide, n8, static_cast<uint4 *>(bvh8q), errw);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, errw, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(wide, st);
+  if (e != cudaSuccess) return e;
+  if (bad) {
+    snprintf(errbuf, errlen, "bvh8: a child box does not fit its node's 8-bit grid");
+    return cudaErrorInvalidValue;
+  }
+  *n8_out = n8;
   *levels_out = levels;
   return cudaSuccess;
 }

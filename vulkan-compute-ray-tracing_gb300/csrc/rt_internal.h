@@ -32,10 +32,11 @@ enum : uint32_t {
 //           rounding.
 //   leaf_tri  original triangle index of leaf k.
 //   bvh8    the same tree with levels folded into nodes of up to eight
-//           children (bvh8.cu): 8 slots of 32 B, (lo.xyz, hi.x),
-//           (hi.yz, ref, 0), filled slots first, breadth-first numbered,
-//           root node 0; inner refs are (node << 3) | (filled slots - 1),
-//           leaf refs the bvh2 ones (~k). Used by the per-lane 8-wide caster.
+//           children (bvh8.cu), 96 B per node: origin, per-axis exponents,
+//           8-bit child bounds rounded outward, child refs; filled slots
+//           first, breadth-first numbered, root node 0; inner refs are
+//           (node << 3) | (filled slots - 1), leaf refs the bvh2 ones (~k).
+//           Used by the per-lane 8-wide caster.
 struct DevScene {
   const rt_triangle *tris;
   const rt_material *mats;
@@ -58,8 +59,10 @@ struct DevScene {
 // ---------------------------------------------------------------- bvh8.cu
 // Node capacity the collapse may need for `ntris` leaves: (4n - 1) / 7 + 1.
 uint32_t bvh8_capacity(uint32_t ntris);
-// Folds d.bvh2 into bvh8 (capacity `cap` nodes); synchronises `st`.
-cudaError_t build_bvh8(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
+// Folds d.bvh2 into quantized bvh8 nodes (96 B each, capacity `cap`
+// nodes); synchronises `st`.
+constexpr size_t kBvh8NodeBytes = 96;
+cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
                        int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st);
 
 // ---------------------------------------------------------------- relayout.cu

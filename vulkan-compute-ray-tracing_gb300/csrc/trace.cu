@@ -309,6 +309,14 @@ __device__ __forceinline__ bool tri_candidate(const float4 *__restrict__ tpre, i
   return !(u < 0.0f || u > 1.0f || v < 0.0f || __fadd_rn(u, v) > 1.0f);
 }
 
+// 2^e as fp32 for e in [-126, 127].
+__device__ __forceinline__ float pow2i(int e) { return __int_as_float((e + 127) << 23); }
+// Byte b of w as fp32, exactly: 2^23 + byte assembled by a byte permute, then
+// 2^23 subtracted.
+__device__ __forceinline__ float qbyte(uint32_t w, int b) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)b)) - 8388608.0f;
+}
+
 constexpr int kPool = 512;       // leaf pool entries per warp (power of two)
 
 // One ray per lane over bvh8 (Ylitie et al., HPG 2017, without the node
@@ -428,20 +436,40 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_wide(DevScene sc, c
     uint32_t leafmask = 0;
     if (ray_i >= 0 && node >= 0) {
       const float closest = ord_inv((uint32_t)(key_v[lane] >> 32));
-      const float4 *N = bvh8 + 16ll * (node >> 3);
+      const float4 *N = bvh8 + 6ll * (node >> 3);
       const int filled = (node & 7) + 1;
+      // The 96-byte quantized node in three 256-bit loads: a child's plane
+      // o + q * 2^e is entered at (o - ray.o) / d + q * (2^e / d), one FMA
+      // per plane on the byte q.
+      float4 q0, q1, q2, q3, q4, q5;
+      load_slot8(N, q0, q1);
+      load_slot8(N + 2, q2, q3);
+      load_slot8(N + 4, q4, q5);
+      const uint32_t ew = __float_as_uint(q0.w);
+      const float sx = r.ix * pow2i((int)(int8_t)(ew & 0xffu));
+      const float sy = r.iy * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
+      const float sz = r.iz * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
+      const float ax = (q0.x - r.o.x) * r.ix, ay = (q0.y - r.o.y) * r.iy, az = (q0.z - r.o.z) * r.iz;
+      const uint32_t qw[12] = {__float_as_uint(q1.x), __float_as_uint(q1.y), __float_as_uint(q1.z),
+                               __float_as_uint(q1.w), __float_as_uint(q2.x), __float_as_uint(q2.y),
+                               __float_as_uint(q2.z), __float_as_uint(q2.w), __float_as_uint(q3.x),
+                               __float_as_uint(q3.y), __float_as_uint(q3.z), __float_as_uint(q3.w)};
+      ref[0] = __float_as_int(q4.x), ref[1] = __float_as_int(q4.y), ref[2] = __float_as_int(q4.z);
+      ref[3] = __float_as_int(q4.w), ref[4] = __float_as_int(q5.x), ref[5] = __float_as_int(q5.y);
+      ref[6] = __float_as_int(q5.z), ref[7] = __float_as_int(q5.w);
       uint32_t key[8];
 #pragma unroll
       for (int s = 0; s < 8; s++) {
         key[s] = 0xffffffffu;
-        ref[s] = INT_MIN;
         if (s < filled) {
-          float4 a, b;
-          load_slot8(N + 2 * s, a, b);
-          ref[s] = __float_as_int(b.z);
-          const float t = slab_enter(r, a.x, a.w, a.y, b.x, a.z, b.y, closest);
-          const bool hit = t < INF;
-          if (hit && ref[s] >= 0) key[s] = (__float_as_uint(t) & ~7u) | (uint32_t)s;
+          const int w = s >> 2, b = s & 3;
+          const float tlx = fmaf(qbyte(qw[0 + w], b), sx, ax), thx = fmaf(qbyte(qw[6 + w], b), sx, ax);
+          const float tly = fmaf(qbyte(qw[2 + w], b), sy, ay), thy = fmaf(qbyte(qw[8 + w], b), sy, ay);
+          const float tlz = fmaf(qbyte(qw[4 + w], b), sz, az), thz = fmaf(qbyte(qw[10 + w], b), sz, az);
+          const float tn = max3f(fminf(tlx, thx), fminf(tly, thy), fmaxf(fminf(tlz, thz), r.tmin));
+          const float tf = min3f(fmaxf(tlx, thx), fmaxf(tly, thy), fminf(fmaxf(tlz, thz), closest));
+          const bool hit = tn <= tf;
+          if (hit && ref[s] >= 0) key[s] = (__float_as_uint(tn) & ~7u) | (uint32_t)s;
           if (hit && ref[s] < 0) leafmask |= 1u << s;
         }
       }
