@@ -61,6 +61,14 @@ uint32_t rtgbGenGrid(uint64_t seed, uint32_t gx, uint32_t gz, uint32_t level, fl
 /* Uniform double in [0,1) from the SplitMix64 stream at (seed, index). */
 double rtgbUniform(uint64_t seed, uint64_t index);
 
+/* Host form of the 8-wide node quantization the scene upload runs on the
+ * GPU: `boxes` holds `filled` (1..8) child boxes as lo.xyz, hi.xyz; `out`
+ * receives the node's 24 words (origin, int8 exponents and count, 8-bit
+ * child bounds, refs). Returns 1, or 0 when a box does not fit the node's
+ * grid. Exposed so the decoded boxes can be checked to contain the
+ * originals without a GPU. */
+uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t filled, uint32_t *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,6 +35,61 @@
 #include "rt_internal.h"
 
 namespace rtgb {
+
+// Quantizes one node: box[s] = (lo.xyz, hi.xyz) of the `filled` children,
+// refs copied as given, into the 24 words of a bvh8 node (layout above).
+// Per axis the origin is the children's union lo and the step the smallest
+// power of two 2^e with extent <= 255 * 2^e; each bound becomes a byte,
+// rounded down for lo and up for hi, then checked in fp64 against the fp32
+// bound and moved outward if needed, so the decoded box o + q * 2^e always
+// contains the original. False when some box does not fit the grid.
+__host__ __device__ inline bool quantize_node8(const float box[8][6], const int32_t ref[8], int filled,
+                                               uint32_t w[24]) {
+  bool ok = filled >= 1 && filled <= 8;
+  if (!ok) filled = 1;
+  for (int i = 0; i < 24; i++) w[i] = 0;
+  uint32_t ebytes = (uint32_t)filled << 24;
+  for (int k = 0; k < 3; k++) {
+    float ulo = box[0][k], uhi = box[0][3 + k];
+    for (int s = 1; s < filled; s++) {
+      ulo = fminf(ulo, box[s][k]);
+      uhi = fmaxf(uhi, box[s][3 + k]);
+    }
+    const double E = (double)uhi - (double)ulo;
+    int e = -126;
+    if (E > 0.0) {
+      int e0 = 0;
+      frexp(E / 255.0, &e0);  // E / 255 <= 2^e0
+      e = (E <= 255.0 * ldexp(1.0, e0 - 1)) ? e0 - 1 : e0;
+      e = e < -126 ? -126 : (e > 127 ? 127 : e);
+    }
+    const double sc = ldexp(1.0, e);
+    if (E > 255.0 * sc) ok = false;
+    for (int s = 0; s < filled; s++) {
+      const double lo = box[s][k], hi = box[s][3 + k];
+      int ql = (int)floor((lo - (double)ulo) / sc);
+      ql = ql < 0 ? 0 : (ql > 255 ? 255 : ql);
+      while (ql > 0 && (double)ulo + ql * sc > lo) ql--;
+      int qh = (int)ceil((hi - (double)ulo) / sc);
+      qh = qh < 0 ? 0 : (qh > 255 ? 255 : qh);
+      while (qh < 255 && (double)ulo + qh * sc < hi) qh++;
+      if ((double)ulo + ql * sc > lo || (double)ulo + qh * sc < hi) ok = false;
+      w[4 + 2 * k + (s >> 2)] |= (uint32_t)ql << (8 * (s & 3));
+      w[10 + 2 * k + (s >> 2)] |= (uint32_t)qh << (8 * (s & 3));
+    }
+    union {
+      float f;
+      uint32_t u;
+    } bits;
+    bits.f = ulo;
+    w[k] = bits.u;
+    ebytes |= ((uint32_t)(e & 0xff)) << (8 * k);
+  }
+  w[3] = ebytes;
+  for (int s = 0; s < 8; s++) w[16 + s] = (uint32_t)ref[s];
+  return ok;
+}
+
 namespace {
 
 struct Slot {
@@ -171,51 +226,18 @@ __global__ void k_quantize8(const float4 *__restrict__ wide, uint32_t n8, uint4 
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= n8) return;
   const float4 *W = wide + 16ull * f;
-  float lo[8][3], hi[8][3];
+  float box[8][6];
   int32_t ref[8];
   int filled = 0;
   for (int s = 0; s < 8; s++) {
     const float4 a = W[2 * s], b = W[2 * s + 1];
-    lo[s][0] = a.x, lo[s][1] = a.y, lo[s][2] = a.z;
-    hi[s][0] = a.w, hi[s][1] = b.x, hi[s][2] = b.y;
+    box[s][0] = a.x, box[s][1] = a.y, box[s][2] = a.z;
+    box[s][3] = a.w, box[s][4] = b.x, box[s][5] = b.y;
     ref[s] = __float_as_int(b.z);
     if (ref[s] != INT_MIN) filled = s + 1;
   }
   uint32_t w[24];
-  for (int i = 0; i < 24; i++) w[i] = 0;
-  uint32_t ebytes = (uint32_t)filled << 24;
-  for (int k = 0; k < 3; k++) {
-    float ulo = lo[0][k], uhi = hi[0][k];
-    for (int s = 1; s < filled; s++) {
-      ulo = fminf(ulo, lo[s][k]);
-      uhi = fmaxf(uhi, hi[s][k]);
-    }
-    const double E = (double)uhi - (double)ulo;
-    int e = -126;
-    if (E > 0.0) {
-      int e0 = 0;
-      frexp(E / 255.0, &e0);  // E / 255 <= 2^e0
-      e = (E <= 255.0 * ldexp(1.0, e0 - 1)) ? e0 - 1 : e0;
-      e = e < -126 ? -126 : (e > 127 ? 127 : e);
-    }
-    const double sc = ldexp(1.0, e);
-    if (E > 255.0 * sc) atomicOr(err, 8u);
-    for (int s = 0; s < filled; s++) {
-      int ql = (int)floor(((double)lo[s][k] - (double)ulo) / sc);
-      ql = ql < 0 ? 0 : (ql > 255 ? 255 : ql);
-      while (ql > 0 && (double)ulo + ql * sc > (double)lo[s][k]) ql--;
-      int qh = (int)ceil(((double)hi[s][k] - (double)ulo) / sc);
-      qh = qh < 0 ? 0 : (qh > 255 ? 255 : qh);
-      while (qh < 255 && (double)ulo + qh * sc < (double)hi[s][k]) qh++;
-      if ((double)ulo + ql * sc > (double)lo[s][k] || (double)ulo + qh * sc < (double)hi[s][k]) atomicOr(err, 8u);
-      w[4 + 2 * k + (s >> 2)] |= (uint32_t)ql << (8 * (s & 3));
-      w[10 + 2 * k + (s >> 2)] |= (uint32_t)qh << (8 * (s & 3));
-    }
-    w[k] = __float_as_uint(ulo);
-    ebytes |= ((uint32_t)(e & 0xff)) << (8 * k);
-  }
-  w[3] = ebytes;
-  for (int s = 0; s < 8; s++) w[16 + s] = (uint32_t)ref[s];
+  if (!quantize_node8(box, ref, filled, w)) atomicOr(err, 8u);
   uint4 *o = out + 6ull * f;
   for (int i = 0; i < 6; i++) o[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
 }
@@ -350,3 +372,16 @@ cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n
 }
 
 }  // namespace rtgb
+
+// Host form of the node quantization, so that its containment guarantee can
+// be checked without a GPU (rt_scenes.h).
+extern "C" uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t filled, uint32_t *out) {
+  if (!boxes || !refs || !out || filled < 1 || filled > 8) return 0;
+  float box[8][6] = {};
+  int32_t ref[8];
+  for (uint32_t s = 0; s < 8; s++) {
+    ref[s] = s < filled ? refs[s] : INT_MIN;
+    for (int j = 0; j < 6; j++) box[s][j] = s < filled ? boxes[6 * s + j] : 0.0f;
+  }
+  return rtgb::quantize_node8(box, ref, (int)filled, out) ? 1u : 0u;
+}

@@ -131,6 +131,7 @@ def _load() -> ctypes.CDLL:
         "rtgbGenRandomRays": (None, [U64, U64, F32, F32, F32, F32, P]),
         "rtgbGenGrid": (U32, [U64, U32, U32, U32, F32, F32, U32, F32, P, P]),
         "rtgbUniform": (ctypes.c_double, [U64, U64]),
+        "rtgbQuantizeNode8": (ctypes.c_uint32, [P, P, U32, P]),
         "rtgbGlibcRand": (None, [U32, U64, P]),
         "rtLoadObj": (I32, [ctypes.c_char_p, U32, P, U32, ctypes.POINTER(U32)]),
         "rtObjLastError": (ctypes.c_char_p, []),
