@@ -319,12 +319,12 @@ __device__ __forceinline__ float qbyte(uint32_t w, int b) {
 
 constexpr int kPool = 512;       // leaf pool entries per warp (power of two)
 
-// One ray per lane over bvh8 (Ylitie et al., HPG 2017, without the node
-// compression): a step tests the filled child slots of the lane's node (up
-// to eight independent 256-bit loads; the count comes with the node's
-// reference), ranks the inner children that are hit by
-// entry distance (pairwise compares), descends into the nearest and pushes
-// the rest onto the lane's stack in near-to-far order. Leaves that are hit
+// One ray per lane over bvh8 (Ylitie et al., HPG 2017, with explicit child
+// refs): a step loads the lane's 96-byte quantized node (three 256-bit
+// loads), tests its filled child slots (the count comes with the node's
+// reference), sorts the inner children that are hit by entry distance,
+// descends into the nearest and pushes the rest onto the lane's stack in
+// near-to-far order. Leaves that are hit
 // go to the warp's FIFO leaf pool in shared memory as (leaf, lane) entries;
 // whenever 32 are pooled, or a lane has run out of nodes with entries still
 // pooled, all 32 lanes test one pooled triangle each against the owning
