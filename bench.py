@@ -280,6 +280,7 @@ def run_gpu(args):
     # Average algorithmic bytes per launch / average launch duration (GB/s).
     achieved = ((alg[0] + alg[1]) / 2) / (((coh_ms + inc_ms) / 2) / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    traffic = traffic_from_profile()
 
     # End to end: host arrays (pinned) through rtTraceClosestHost.
     h_rays = [torch.from_numpy(coherent).pin_memory(), torch.from_numpy(incoherent).pin_memory()]
@@ -315,7 +316,10 @@ def run_gpu(args):
                    "incoherent_grays": RAYS_PER_BATCH / inc_ms / 1e6, "bvh_build_ms": info.build_ms,
                    "bvh_depth": info.depth},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic_from_profile(), "peak_kind": peak_kind,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     # DRAM bytes per ray actually moved (ncu), beside the
+                     # algorithmic bytes: frac > 1 is L1/L2 reuse.
+                     "dram_bytes_per_ray": traffic / RAYS_PER_BATCH if traffic else None,
                      "alg_bytes_per_ray": {"coherent": ALG_BYTES_COHERENT, "incoherent": ALG_BYTES_INCOHERENT}},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_step * 32,
                 "d2h_bytes_per_step": rays_step * 16, "matches_device_path": bool(same)},
