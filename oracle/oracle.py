@@ -44,6 +44,8 @@ def _load():
         "oracle_render": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
         "oracle_render_f64": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
         "oracle_max_threads": (I32, []),
+        "oracle_wide_fold": (I32, [P, U32, U32, P, P, P, ctypes.POINTER(U32), ctypes.POINTER(U32)]),
+        "oracle_trace_wide": (I32, [P, U32, P, U32, I32, P, P, U32, P, I32]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -284,6 +286,40 @@ def trace(tris, nodes, rays, mode: int = 0, stack_size: int = 16, slack: float =
     LIB.oracle_trace(_p(tris), len(tris), _p(nodes), len(nodes), _p(rays), len(rays), mode, stack_size, slack,
                      _p(hits), _p(st), threads)
     return (hits, st) if stats else hits
+
+
+def wide_fold(nodes):
+    """The GPU builder's 8-wide fold of a reference node array, restated:
+    per node up to 8 child boxes (lo.xyz, hi.xyz), refs ((node << 3) |
+    (filled - 1) for inner children, ~triangle for leaves, INT_MIN empty)
+    and the filled count. Returns (boxes (n8, 8, 6), refs (n8, 8), filled,
+    levels)."""
+    nodes = np.ascontiguousarray(nodes, np.float32)
+    cap = max(1, (4 * ((len(nodes) + 1) // 2) + 6) // 7 + 1)
+    boxes = np.zeros((cap, 8, 6), np.float32)
+    refs = np.zeros((cap, 8), np.int32)
+    filled = np.zeros(cap, np.uint32)
+    n8, levels = ctypes.c_uint32(0), ctypes.c_uint32(0)
+    rc = LIB.oracle_wide_fold(_p(nodes), len(nodes), cap, _p(boxes), _p(refs), _p(filled), ctypes.byref(n8),
+                              ctypes.byref(levels))
+    if rc != 0:
+        raise RuntimeError(f"oracle_wide_fold failed ({rc})")
+    n = n8.value
+    return boxes[:n], refs[:n], filled[:n], levels.value
+
+
+def trace_wide(tris, qwords, root8: int, root_box, rays, threads: int = 0) -> np.ndarray:
+    """Closest hits through quantized 8-wide nodes (qwords: (n8, 24) uint32),
+    with the GPU kernel's plane arithmetic; hits as oracle `trace`."""
+    tris, rays = np.ascontiguousarray(tris, np.float32), np.ascontiguousarray(rays, np.float32)
+    qwords = np.ascontiguousarray(qwords, np.uint32)
+    rb = np.ascontiguousarray(root_box, np.float32)
+    hits = np.zeros((len(rays), 4), np.float32)
+    rc = LIB.oracle_trace_wide(_p(tris), len(tris), _p(qwords), len(qwords), root8, _p(rb), _p(rays), len(rays),
+                               _p(hits), threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle_trace_wide failed ({rc})")
+    return hits
 
 
 def trace_f64(tris, nodes, rays, threads: int = 0):

@@ -810,4 +810,215 @@ void oracle_denoise(const float *in, uint32_t W, uint32_t H, float sigma, float 
     }
   }
 }
+
+// ---------------------------------------------------------------- 8-wide model
+// A host model of the GPU's 8-wide closest-hit traversal, used to check its
+// central claim on many scenes without a GPU: pruning by quantized 8-bit
+// child boxes, with the kernel's fp32 plane arithmetic, never drops the
+// closest hit. oracle_wide_fold folds the reference node array into nodes
+// of up to eight children with the GPU builder's rule (replace the inner
+// child of largest half area, dx*dy + dy*dz + dz*dx, by its two children,
+// left in place and right appended, first of equal areas) and breadth-first
+// numbering; inner refs are (node << 3) | (filled - 1), leaf refs
+// ~triangle. The caller quantizes each node with the library's host
+// quantizer (96-byte words) and oracle_trace_wide traverses those words:
+// planes entered at fmaf(q, ix * 2^e, (o - ray.o) * ix), children sorted
+// near-first, triangles tested when reached with the acceptance rule of the
+// culled traversal (exactly equal t: the lower triangle index wins).
+int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, float *boxes, int32_t *refs,
+                     uint32_t *filled_out, uint32_t *n8_out, uint32_t *levels_out) {
+  if (!nodes || nnodes == 0 || !boxes || !refs || !filled_out || !n8_out) return 1;
+  struct Slot {
+    float b[6];
+    int32_t node;  // reference node index
+  };
+  auto slot_of = [&](int32_t i) {
+    Slot s;
+    for (int k = 0; k < 3; k++) {
+      s.b[k] = nodes[i].min[k];
+      s.b[3 + k] = nodes[i].max[k];
+    }
+    s.node = i;
+    return s;
+  };
+  auto inner = [&](int32_t i) { return nodes[i].left != -1; };
+  auto area = [](const Slot &s) {
+    float dx = s.b[3] - s.b[0], dy = s.b[4] - s.b[1], dz = s.b[5] - s.b[2];
+    return dx * dy + dy * dz + dz * dx;
+  };
+  std::vector<int32_t> frontier, next;
+  std::vector<std::vector<Slot>> built;
+  uint32_t levels = 0;
+  if (!inner(0)) {
+    built.push_back({slot_of(0)});
+  } else {
+    frontier.push_back(0);
+    while (!frontier.empty()) {
+      next.clear();
+      for (int32_t f : frontier) {
+        std::vector<Slot> S = {slot_of(nodes[f].left), slot_of(nodes[f].right)};
+        while (S.size() < 8) {
+          int pick = -1;
+          float best = -1.0f;
+          for (size_t i = 0; i < S.size(); i++) {
+            if (!inner(S[i].node)) continue;
+            float a = area(S[i]);
+            if (a > best) {
+              best = a;
+              pick = (int)i;
+            }
+          }
+          if (pick < 0) break;
+          int32_t p = S[pick].node;
+          S[pick] = slot_of(nodes[p].left);
+          S.push_back(slot_of(nodes[p].right));
+        }
+        built.push_back(S);
+        for (const Slot &c : S)
+          if (inner(c.node)) next.push_back(c.node);
+      }
+      frontier.swap(next);
+      levels++;
+    }
+  }
+  if (built.size() > cap) return 2;
+  // Node numbers: breadth first, the inner children of node i in slot order.
+  std::vector<uint32_t> first_child(built.size());
+  uint32_t counter = 1;
+  for (size_t i = 0; i < built.size(); i++) {
+    first_child[i] = counter;
+    for (const Slot &c : built[i]) counter += inner(c.node) ? 1u : 0u;
+  }
+  for (size_t i = 0; i < built.size(); i++) {
+    uint32_t c = first_child[i];
+    filled_out[i] = (uint32_t)built[i].size();
+    for (int s = 0; s < 8; s++) {
+      float *b = boxes + 6 * (8 * i + s);
+      if (s >= (int)built[i].size()) {
+        for (int k = 0; k < 6; k++) b[k] = 0.0f;
+        refs[8 * i + s] = INT32_MIN;
+        continue;
+      }
+      const Slot &sl = built[i][s];
+      for (int k = 0; k < 6; k++) b[k] = sl.b[k];
+      if (inner(sl.node)) {
+        refs[8 * i + s] = (int32_t)c;  // encoded with the child's count below
+        c++;
+      } else {
+        refs[8 * i + s] = ~nodes[sl.node].object;
+      }
+    }
+  }
+  for (size_t i = 0; i < built.size(); i++)
+    for (int s = 0; s < 8; s++) {
+      int32_t r = refs[8 * i + s];
+      if (r >= 0) refs[8 * i + s] = (r << 3) | (int32_t)(built[r].size() - 1);
+    }
+  *n8_out = (uint32_t)built.size();
+  if (levels_out) *levels_out = levels;
+  return 0;
+}
+
+static inline float safe_rcp_model(float x) {
+  const float tiny = 1e-30f;
+  return 1.0f / (std::fabs(x) > tiny ? x : std::copysign(tiny, x));
+}
+
+int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *qwords, uint32_t n8, int32_t root8,
+                      const float *root_box, const rt_ray *rays, uint32_t nrays, rt_hit *hits, int threads) {
+  if (!tris || !qwords || !root_box || !rays || !hits || n8 == 0) return 1;
+  if (threads > 0) omp_set_num_threads(threads);
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(| : bad)
+  for (int64_t i = 0; i < (int64_t)nrays; i++) {
+    const rt_ray &r = rays[i];
+    const float ix = safe_rcp_model(r.d[0]), iy = safe_rcp_model(r.d[1]), iz = safe_rcp_model(r.d[2]);
+    const float inv[3] = {ix, iy, iz};
+    const float oi[3] = {r.o[0] * ix, r.o[1] * iy, r.o[2] * iz};
+    float closest = r.tmax, bu = 0, bv = 0;
+    int32_t best = -1;
+    // Root box: the kernels' slab test, fmaf(lo, 1/d, -o/d).
+    float tn = r.tmin, tf = closest;
+    for (int k = 0; k < 3; k++) {
+      const float a = std::fmaf(root_box[k], inv[k], -oi[k]), b = std::fmaf(root_box[3 + k], inv[k], -oi[k]);
+      tn = std::fmax(tn, std::fmin(a, b));
+      tf = std::fmin(tf, std::fmax(a, b));
+    }
+    std::vector<int32_t> stack;
+    int32_t node = tn <= tf ? root8 : -1;
+    uint32_t steps = 0;
+    while (node >= 0 || !stack.empty()) {
+      if (node < 0) {
+        node = stack.back();
+        stack.pop_back();
+      }
+      const uint32_t idx = (uint32_t)node >> 3;
+      const int filled = (node & 7) + 1;
+      if (idx >= n8 || ++steps > n8 + 16) {
+        bad = 1;
+        break;
+      }
+      const uint32_t *w = qwords + 24ull * idx;
+      float org[3];
+      std::memcpy(org, w, 12);
+      float sc[3], ax[3];
+      for (int k = 0; k < 3; k++) {
+        const int e = (int)(int8_t)((w[3] >> (8 * k)) & 0xffu);
+        float p2;
+        const uint32_t pb = (uint32_t)(e + 127) << 23;
+        std::memcpy(&p2, &pb, 4);
+        sc[k] = inv[k] * p2;
+        ax[k] = (org[k] - r.o[k]) * inv[k];
+      }
+      uint32_t key[8];
+      int32_t ref[8];
+      for (int s = 0; s < 8; s++) {
+        key[s] = 0xffffffffu;
+        ref[s] = (int32_t)w[16 + s];
+        if (s >= filled) continue;
+        float t[6];
+        for (int k = 0; k < 3; k++) {
+          const float ql = (float)((w[4 + 2 * k + (s >> 2)] >> (8 * (s & 3))) & 0xffu);
+          const float qh = (float)((w[10 + 2 * k + (s >> 2)] >> (8 * (s & 3))) & 0xffu);
+          t[k] = std::fmaf(ql, sc[k], ax[k]);
+          t[3 + k] = std::fmaf(qh, sc[k], ax[k]);
+        }
+        const float n0 = std::fmax(std::fmax(std::fmin(t[0], t[3]), std::fmin(t[1], t[4])),
+                                   std::fmax(std::fmin(t[2], t[5]), r.tmin));
+        const float f0 = std::fmin(std::fmin(std::fmax(t[0], t[3]), std::fmax(t[1], t[4])),
+                                   std::fmin(std::fmax(t[2], t[5]), closest));
+        if (!(n0 <= f0)) continue;
+        if (ref[s] >= 0) {
+          uint32_t b;
+          std::memcpy(&b, &n0, 4);
+          key[s] = (b & ~7u) | (uint32_t)s;
+        } else {
+          const int32_t tri = ~ref[s];
+          if (tri < 0 || (uint32_t)tri >= ntris) {
+            bad = 1;
+            continue;
+          }
+          float t0, u, v;
+          V3<float> n;
+          if (!tri_intersect<float>(tris[tri], ld3<float>(r.o), ld3<float>(r.d), t0, u, v, n)) continue;
+          if (!(t0 > r.tmin && t0 < r.tmax)) continue;
+          if (t0 < closest || (best >= 0 && t0 == closest && tri < best)) {
+            closest = t0;
+            best = tri;
+            bu = u;
+            bv = v;
+          }
+        }
+      }
+      std::sort(key, key + 8);
+      node = -1;
+      int cnt = 0;
+      while (cnt < 8 && key[cnt] != 0xffffffffu) cnt++;
+      for (int j = cnt - 1; j >= 1; j--) stack.push_back(ref[key[j] & 7u]);
+      if (cnt > 0) node = ref[key[0] & 7u];
+    }
+    hits[i] = best >= 0 ? rt_hit{best, closest, bu, bv} : rt_hit{-1, 0.0f, 0.0f, 0.0f};
+  }
+  return bad ? 3 : 0;
+}
 }

@@ -1,0 +1,121 @@
+"""The GPU's 8-wide closest-hit traversal checked on the host.
+
+The oracle restates the fold (oracle_wide_fold, the GPU builder's greedy
+rule) and the traversal (oracle_trace_wide: the kernel's fp32 plane
+arithmetic on quantized nodes, near-first order, the triangle-index tie
+rule); the nodes are quantized by the library's own host quantizer
+(rtgbQuantizeNode8, the function the upload runs on the GPU). The hits
+must equal the oracle's culled binary traversal bit for bit: pruning by
+8-bit boxes rounded outward never drops the closest hit. Leaves are tested
+as soon as they are reached (the GPU pools them), which prunes harder and so
+checks the containment more strictly."""
+import numpy as np
+import pytest
+
+
+def quantize_all(rt, boxes, refs, filled):
+    words = np.zeros((len(boxes), 24), np.uint32)
+    out = np.zeros(24, np.uint32)
+    for i in range(len(boxes)):
+        n = int(filled[i])
+        b = np.ascontiguousarray(boxes[i, :n], np.float32)
+        r = np.ascontiguousarray(refs[i, :n], np.int32)
+        assert rt.LIB.rtgbQuantizeNode8(b.ctypes.data, r.ctypes.data, n, out.ctypes.data) == 1
+        words[i] = out
+    return words
+
+
+def wide_hits(rt, orc, tris, nodes, rays):
+    boxes, refs, filled, levels = orc.wide_fold(nodes)
+    assert levels >= 1 and (filled >= 1).all() and (filled <= 8).all()
+    # Every triangle sits in exactly one leaf slot.
+    leaves = refs[refs < 0]
+    leaves = leaves[leaves != np.iinfo(np.int32).min]
+    assert sorted((~leaves).tolist()) == list(range(len(tris)))
+    words = quantize_all(rt, boxes, refs, filled)
+    root8 = (0 << 3) | (int(filled[0]) - 1) if nodes.view(np.int32)[0, 7] != -1 else 0
+    root_box = np.concatenate([nodes[0, 0:3], nodes[0, 4:7]]).astype(np.float32)
+    return orc.trace_wide(tris, words, root8, root_box, rays)
+
+
+def check(rt, orc, tris, rays):
+    nodes, _ = orc.build_bvh(tris, 1)
+    want = orc.trace(tris, nodes, rays)
+    got = wide_hits(rt, orc, tris, nodes, rays)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert (want.view(np.int32)[:, 0] >= 0).mean() > 0.2
+
+
+def test_icosphere_camera_and_random(rt, orc):
+    tris = rt.gen_icosphere(2, 5)
+    cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 96, 96)
+    rays = np.concatenate([rt.gen_camera_rays(cam, 96, 96), rt.gen_random_rays(5, 20000)])
+    check(rt, orc, tris, rays)
+
+
+def test_cornell_rays_from_inside(rt, orc):
+    t, _, _ = rt.gen_cornell(3, 4000, 0)
+    rays = rt.gen_random_rays(7, 20000, -4.0, 4.0)
+    check(rt, orc, t, rays)
+
+
+@pytest.mark.parametrize("offset,scale", [((1000.0, -2000.0, 500.0), 10.0), ((-3.0e4, 0.0, 7.0), 1.0),
+                                          ((0.0, 0.0, 0.0), 1e-3)])
+def test_offset_and_scaled_mesh(rt, orc, offset, scale):
+    tris = rt.gen_icosphere(4, 4).copy()
+    off = np.array(offset, np.float32)
+    for v in range(3):
+        tris[:, 4 * v:4 * v + 3] = tris[:, 4 * v:4 * v + 3] * np.float32(scale) + off
+    rays = rt.gen_random_rays(9, 8000).copy()
+    rays[:, 0:3] = rays[:, 0:3] * np.float32(scale) + off
+    rays[:, 3] = 0.0
+    check(rt, orc, tris, rays)
+
+
+def test_axis_aligned_rays(rt, orc):
+    """Direction components of exactly 0 take the clamped 1/d path."""
+    tris = rt.gen_icosphere(6, 4)
+    rng = np.random.default_rng(3)
+    n = 6000
+    rays = np.zeros((n, 8), np.float32)
+    axis = rng.integers(0, 3, n)
+    sign = rng.choice([-1.0, 1.0], n)
+    rays[:, 0:3] = rng.uniform(-0.8, 0.8, (n, 3))
+    rays[np.arange(n), axis] = -1.5 * sign
+    rays[np.arange(n), 4 + axis] = sign
+    rays[:, 3] = 1e-4
+    rays[:, 7] = np.inf
+    check(rt, orc, tris, rays)
+
+
+def test_deep_tree_bench_mesh_family(rt, orc):
+    """The displaced icosphere of the closest-hit workload at level 7
+    (327,680 triangles, a fold of ~11 levels), camera and random rays."""
+    tris = rt.gen_icosphere(1, 7)
+    cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 64, 64)
+    rays = np.concatenate([rt.gen_camera_rays(cam, 64, 64), rt.gen_random_rays(3, 8192)])
+    check(rt, orc, tris, rays)
+
+
+def test_model_detects_shrunk_boxes(rt, orc):
+    """Sensitivity: the same traversal over boxes shrunk by one grid step
+    (every upper byte lowered by 1, a non-conservative quantization) must
+    lose hits; the check above would catch a quantizer that rounds inward."""
+    tris = rt.gen_icosphere(2, 5)
+    nodes, _ = orc.build_bvh(tris, 1)
+    rays = rt.gen_random_rays(5, 20000)
+    want = orc.trace(tris, nodes, rays)
+    boxes, refs, filled, _ = orc.wide_fold(nodes)
+    words = quantize_all(rt, boxes, refs, filled)
+    for wi in range(10, 16):  # the qhi words
+        w = words[:, wi].copy()
+        out = np.zeros_like(w)
+        for b in range(4):
+            byte = (w >> np.uint32(8 * b)) & np.uint32(0xFF)
+            byte = np.where(byte > 0, byte - 1, byte)
+            out |= byte << np.uint32(8 * b)
+        words[:, wi] = out
+    root8 = (int(filled[0]) - 1)
+    root_box = np.concatenate([nodes[0, 0:3], nodes[0, 4:7]]).astype(np.float32)
+    got = orc.trace_wide(tris, words, root8, root_box, rays)
+    assert not np.array_equal(got.view(np.uint32), want.view(np.uint32))
