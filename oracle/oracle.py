@@ -45,7 +45,7 @@ def _load():
         "oracle_render_f64": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
         "oracle_max_threads": (I32, []),
         "oracle_wide_fold": (I32, [P, U32, U32, P, P, P, ctypes.POINTER(U32), ctypes.POINTER(U32)]),
-        "oracle_trace_wide": (I32, [P, U32, P, U32, I32, P, P, U32, P, I32]),
+        "oracle_trace_wide": (I32, [P, U32, P, U32, I32, P, P, U32, P, P, I32]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -308,18 +308,20 @@ def wide_fold(nodes):
     return boxes[:n], refs[:n], filled[:n], levels.value
 
 
-def trace_wide(tris, qwords, root8: int, root_box, rays, threads: int = 0) -> np.ndarray:
+def trace_wide(tris, qwords, root8: int, root_box, rays, threads: int = 0, stats: bool = False):
     """Closest hits through quantized 8-wide nodes (qwords: (n8, 24) uint32),
-    with the GPU kernel's plane arithmetic; hits as oracle `trace`."""
+    with the GPU kernel's plane arithmetic; hits as oracle `trace`, and with
+    stats=True also (n, 2) uint32: nodes visited, triangles tested."""
     tris, rays = np.ascontiguousarray(tris, np.float32), np.ascontiguousarray(rays, np.float32)
     qwords = np.ascontiguousarray(qwords, np.uint32)
     rb = np.ascontiguousarray(root_box, np.float32)
     hits = np.zeros((len(rays), 4), np.float32)
+    st = np.zeros((len(rays), 2), np.uint32) if stats else None
     rc = LIB.oracle_trace_wide(_p(tris), len(tris), _p(qwords), len(qwords), root8, _p(rb), _p(rays), len(rays),
-                               _p(hits), threads)
+                               _p(hits), _p(st), threads)
     if rc != 0:
         raise RuntimeError(f"oracle_trace_wide failed ({rc})")
-    return hits
+    return (hits, st) if stats else hits
 
 
 def trace_f64(tris, nodes, rays, threads: int = 0):

@@ -924,8 +924,10 @@ static inline float safe_rcp_model(float x) {
   return 1.0f / (std::fabs(x) > tiny ? x : std::copysign(tiny, x));
 }
 
+// stats (optional): per ray, nodes visited and triangles tested.
 int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *qwords, uint32_t n8, int32_t root8,
-                      const float *root_box, const rt_ray *rays, uint32_t nrays, rt_hit *hits, int threads) {
+                      const float *root_box, const rt_ray *rays, uint32_t nrays, rt_hit *hits, uint32_t *stats,
+                      int threads) {
   if (!tris || !qwords || !root_box || !rays || !hits || n8 == 0) return 1;
   if (threads > 0) omp_set_num_threads(threads);
   int bad = 0;
@@ -946,7 +948,7 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
     }
     std::vector<int32_t> stack;
     int32_t node = tn <= tf ? root8 : -1;
-    uint32_t steps = 0;
+    uint32_t steps = 0, ntests = 0;
     while (node >= 0 || !stack.empty()) {
       if (node < 0) {
         node = stack.back();
@@ -1000,6 +1002,7 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
           }
           float t0, u, v;
           V3<float> n;
+          ntests++;
           if (!tri_intersect<float>(tris[tri], ld3<float>(r.o), ld3<float>(r.d), t0, u, v, n)) continue;
           if (!(t0 > r.tmin && t0 < r.tmax)) continue;
           if (t0 < closest || (best >= 0 && t0 == closest && tri < best)) {
@@ -1018,6 +1021,10 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
       if (cnt > 0) node = ref[key[0] & 7u];
     }
     hits[i] = best >= 0 ? rt_hit{best, closest, bu, bv} : rt_hit{-1, 0.0f, 0.0f, 0.0f};
+    if (stats) {
+      stats[2 * i] = steps;
+      stats[2 * i + 1] = ntests;
+    }
   }
   return bad ? 3 : 0;
 }
