@@ -6,7 +6,7 @@ built from the reference's src/ray-tracing/Bvh.h) and its own compute shader
 (_ref/libref_shader.so, ray-trace-compute.comp rewritten into C++ by
 glsl2cpp.py). Only the tests,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module,
-and only as the checker / the timed CPU baseline.
+and only as the oracle / the timed CPU baseline.
 """
 from __future__ import annotations
 

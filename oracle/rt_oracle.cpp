@@ -1,8 +1,8 @@
 // Test infrastructure (oracle) — NOT part of the product.
 //
 // A CPU restatement of the reference's ray-trace hot path, used only by the
-// tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the
-// checker. Nothing in the product links, loads or calls this file.
+// tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, as the
+// oracle. Nothing in the product links, loads or calls this file.
 //
 // What it restates (reference paths relative to the reference checkout):
 //   * Bvh::createBvh            src/ray-tracing/Bvh.h:141-209 (with helpers 16-122)

@@ -7,8 +7,8 @@ rule); the nodes are quantized by the library's own host quantizer
 (rtgbQuantizeNode8, the function the upload runs on the GPU). The hits
 must equal the oracle's culled binary traversal bit for bit: pruning by
 8-bit boxes rounded outward never drops the closest hit. Leaves are tested
-as soon as they are reached (the GPU pools them), which prunes harder and so
-checks the containment more strictly."""
+as soon as they are reached (the kernel collects them in a shared pool
+first), which prunes harder and so checks the containment more strictly."""
 import numpy as np
 import pytest
 

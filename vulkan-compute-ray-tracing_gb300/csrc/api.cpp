@@ -283,7 +283,7 @@ rt_status rtCameraLookAt(const float eye[3], const float target[3], const float 
   if (!eye || !target || !up || !out || W == 0 || H == 0 || !(vfov_deg > 0.0f && vfov_deg < 180.0f))
     return RT_ERR_INVALID_ARGUMENT;
   // Computed in double and rounded once: the camera is an input to both
-  // the kernels and any checker, so only its stored fp32 values matter.
+  // the kernels and the oracle, so only its stored fp32 values matter.
   double f[3], r[3], u[3];
   for (int a = 0; a < 3; a++) f[a] = (double)target[a] - (double)eye[a];
   double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
