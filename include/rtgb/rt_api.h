@@ -214,6 +214,10 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   the reference's tree, but closest hits are identical
  *                   (equal-t ties go to the lower triangle index in every
  *                   tree); rtDownloadBvh returns the tree that was built
+ *   "bvh.test_error_level"  test hook (default -1, off): builder 0 records
+ *                   an error bit in its device error word after the sort of
+ *                   this tree level, as a sort overflow would, so the upload
+ *                   must fail with RT_ERR_INTERNAL
  * Values persist for the context; rtAutotuneTrace / rtAutotuneRender write
  * them. Unknown keys return RT_ERR_INVALID_ARGUMENT. */
 rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);
@@ -254,16 +258,21 @@ rt_status rtReadSegmentCounter(rt_ctx *ctx, uint64_t *out, int reset);
  * where cudaMalloc is forbidden. It allocates nothing: its scratch is a
  * fixed array inside the library (about 3.9 MB on every GPU that loads the
  * library, held until the process exits) plus static host buffers.
- *   d_triangles  n triangles in device memory (Bvh.h layout, finite vertices)
+ *   d_triangles  n triangles in device memory (Bvh.h layout); a vertex
+ *                coordinate that is NaN or infinite returns
+ *                RT_ERR_INVALID_SCENE before any sorting starts
  *   n            1 .. 65536; larger n returns RT_ERR_INVALID_ARGUMENT
  *   bvh_seed     the rand() seed, as in rtUploadScene (the reference: 1)
  *   d_nodes      2n-1 nodes of device memory receiving the Bvh.h node array
  *   stream       cudaStream_t (NULL: the legacy default stream)
- * Returns once the nodes are written. The first call on a device looks up
- * the array's device address (make it before any stream capture). Calls
- * share the array: they are serialised inside the library, and work that
- * overlaps a call on the same device from outside it races. Both pointers
- * must be 16-byte aligned. */
+ * Returns once the nodes are written, and on every error path only after the
+ * work it queued has finished. The first call on each device, with that
+ * device current, looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture
+ * begins. Calls share the array, which keeps the last call's contents: they
+ * are serialised inside the library, and GPU work that overlaps a call on
+ * the same device from outside the library and touches the array races.
+ * Both pointers must be 16-byte aligned. */
 rt_status rtBuildBvhNoAlloc(const rt_triangle *d_triangles, uint32_t n, uint32_t bvh_seed, rt_bvh_node *d_nodes,
                             void *stream);
 

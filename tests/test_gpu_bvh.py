@@ -76,3 +76,20 @@ def test_uploaded_nodes_are_used_as_is(rt, orc, ctx):
         assert np.array_equal(sc.bvh().view(np.uint32)[:, NODE_COLS], nodes.view(np.uint32)[:, NODE_COLS])
     finally:
         sc.release()
+
+
+@pytest.mark.parametrize("level", [0, 3, 9])
+def test_error_raised_at_an_early_level_fails_the_upload(rt, ctx, level):
+    # The build's error word must survive the later levels: a bit recorded
+    # after the sort of `level` (test hook, as an overflow would record it)
+    # fails the upload with RT_ERR_INTERNAL, and the next upload succeeds.
+    tris = rt.gen_cornell(3, 4000)[0]
+    ctx.set_tuning("bvh.test_error_level", level)
+    try:
+        with pytest.raises(rt.RtError) as ei:
+            ctx.upload_scene(tris, _mats(rt))
+        assert ei.value.status == 10
+    finally:
+        ctx.set_tuning("bvh.test_error_level", -1)
+    sc = ctx.upload_scene(tris, _mats(rt))
+    sc.release()

@@ -10,6 +10,7 @@ Usage: ``python build.py`` (or ``import build; build.build()``).
 from __future__ import annotations
 
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -48,9 +49,25 @@ def _compile(src: str, nvcc: str) -> str:
     return obj
 
 
-def _stale(srcs: list[str]) -> bool:
-    if not os.path.exists(LIB):
+STAMP = os.path.join(HERE, "_build", "librtgb.stamp")
+
+
+def _toolchain_id(nvcc: str) -> str:
+    """Machine architecture and nvcc version: a library built elsewhere (a
+    copy from another host, or another toolkit) is stale whatever its mtime."""
+    try:
+        ver = subprocess.run([nvcc, "--version"], capture_output=True, text=True).stdout.strip().splitlines()[-1]
+    except Exception:
+        ver = "unknown"
+    return f"{platform.machine()} {ver} {ARCH}"
+
+
+def _stale(srcs: list[str], nvcc: str) -> bool:
+    if not os.path.exists(LIB) or not os.path.exists(STAMP):
         return True
+    with open(STAMP) as f:
+        if f.read().strip() != _toolchain_id(nvcc):
+            return True
     t = os.path.getmtime(LIB)
     deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     inc = os.path.join(ROOT, "include", "rtgb")
@@ -62,9 +79,9 @@ def _stale(srcs: list[str]) -> bool:
 def build(force: bool = False, jobs: int | None = None) -> str:
     """Compile librtgb.so if any source changed; returns its path."""
     srcs = _sources()
-    if not force and not _stale(srcs):
-        return LIB
     nvcc = _nvcc()
+    if not force and not _stale(srcs, nvcc):
+        return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     with ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, nvcc), srcs))
@@ -74,6 +91,8 @@ def build(force: bool = False, jobs: int | None = None) -> str:
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(_toolchain_id(nvcc) + "\n")
     return LIB
 
 

@@ -415,10 +415,11 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   if (nodes) {
     UCK(cudaMemcpyAsync(dnodes, nodes, sizeof(rt_bvh_node) * nnodes, cudaMemcpyHostToDevice, st), "upload nodes");
   } else {
-    int builder = 0;
+    int builder = 0, test_error_level = -1;
     {
       std::lock_guard<std::mutex> g(ctx->mu);
       builder = ctx->build_opts.builder;
+      test_error_level = ctx->build_opts.test_error_level;
     }
     char errbuf[256] = {0};
     rt_status bs;
@@ -432,7 +433,7 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
       std::vector<uint8_t> axes(nnodes);
       glibc_rand_axes(bvh_seed, nnodes, axes.data());
       bs = gpu_build_bvh((const rt_triangle *)(slab + off_tris), nt, axes.data(), dnodes, st, &sc->build_ms, &depth,
-                         errbuf, sizeof(errbuf));
+                         errbuf, sizeof(errbuf), test_error_level);
     }
     if (bs != RT_SUCCESS) return abort_upload(fail(ctx, bs, "%s", errbuf));
   }
@@ -795,6 +796,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->build_opts.builder = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "bvh.test_error_level") {
+    if (value < -1 || value > 64) return RT_ERR_INVALID_ARGUMENT;
+    ctx->build_opts.test_error_level = (int)value;
+    return RT_SUCCESS;
+  }
   ctx->last_error = "rtSetTuning: unknown key " + k;
   return RT_ERR_INVALID_ARGUMENT;
 }
@@ -861,6 +867,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "bvh.builder") {
     *value = ctx->build_opts.builder;
+    return RT_SUCCESS;
+  }
+  if (k == "bvh.test_error_level") {
+    *value = ctx->build_opts.test_error_level;
     return RT_SUCCESS;
   }
   return RT_ERR_INVALID_ARGUMENT;

@@ -75,6 +75,23 @@ __global__ void k_iota(uint32_t *idx, uint32_t n) {
   if (i < n) idx[i] = i;
 }
 
+// Test hook of the build's error word: records `bits` as a sort kernel
+// would on an overflow, so a test can check that an error raised at any
+// level survives to the end of the build.
+__global__ void k_flag_error(uint32_t *err, uint32_t bits) { atomicOr(err, bits); }
+
+// Every vertex coordinate must be finite: the sort replay orders keys with
+// IEEE `<`, which a NaN key breaks, and node boxes are min/max unions. Any
+// non-finite coordinate sets `bits` in the error word.
+__global__ void k_check_finite(const rt_triangle *__restrict__ tris, uint32_t n, uint32_t *err, uint32_t bits) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const rt_triangle t = tris[i];
+  bool ok = true;
+  for (int k = 0; k < 3; k++) ok = ok && isfinite(t.v0[k]) && isfinite(t.v1[k]) && isfinite(t.v2[k]);
+  if (!ok) atomicOr(err, bits);
+}
+
 // Key of every element that belongs to a node of this level with n >= 2.
 __global__ void k_keys(const Seg *__restrict__ segs, uint32_t nseg, const rt_triangle *__restrict__ tris,
                        const uint32_t *__restrict__ idx, float *__restrict__ key, uint32_t n) {
@@ -510,7 +527,8 @@ HostTopo host_topology(uint32_t n, const uint8_t *axes) {
 }  // namespace
 
 rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_axes, rt_bvh_node *d_nodes,
-                        cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen) {
+                        cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen,
+                        int test_error_level) {
   rt_status status = RT_SUCCESS;
   HostTopo topo = host_topology(n, h_axes);
   float *key = nullptr;
@@ -538,13 +556,16 @@ rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_
   BUILD_CHECK(cudaMemcpyAsync(dleaves, topo.leaves.data(), sizeof(Leaf) * topo.leaves.size(),
                               cudaMemcpyHostToDevice, st));
   BUILD_CHECK(cudaEventRecord(e0, st));
+  // ctr: [0] queue count, [1] queue head (both per level), [2] error bits
+  // (kept across levels), [3] unused.
+  BUILD_CHECK(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 4, st));
   k_iota<<<(n + 255) / 256, 256, 0, st>>>(idx, n);
   for (uint32_t L = 0; L < topo.levels; L++) {
     uint32_t s0 = topo.level_off[L], s1 = topo.level_off[L + 1];
     uint32_t ns = s1 - s0;
     if (ns == 0) continue;
     const Seg *ls = dsegs + s0;
-    BUILD_CHECK(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 4, st));
+    BUILD_CHECK(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 2, st));
     k_keys<<<(n + 255) / 256, 256, 0, st>>>(ls, ns, d_tris, idx, key, n);
     k_enqueue<<<(ns + 255) / 256, 256, 0, st>>>(ls, ns, queue, ctr);
     // Inner nodes of one level have sizes floor or ceil of n / 2^L.
@@ -555,6 +576,7 @@ rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_
     }
     uint32_t grid = (uint32_t)sms * 8u;
     k_sort_warps<<<grid, 256, 0, st>>>(key, idx, P, Q, queue, ctr, ctr + 1, ctr + 2);
+    if ((int)L == test_error_level) k_flag_error<<<1, 1, 0, st>>>(ctr + 2, KERR_STACK_OVERFLOW);
     BUILD_CHECK(cudaGetLastError());
   }
   k_leaves<<<((uint32_t)topo.leaves.size() + 255) / 256, 256, 0, st>>>(dleaves, (uint32_t)topo.leaves.size(),
@@ -711,13 +733,29 @@ extern "C" rt_status rtBuildBvhNoAlloc(const rt_triangle *d_triangles, uint32_t 
   NaHost &h = g_na_host;
   glibc_rand_axes(bvh_seed, 2ull * n - 1, h.axes);
   na_topology(n, h);
+  // From the first enqueue on, every return waits for the work already
+  // queued on `st`: the next call (under the same lock, possibly on another
+  // stream) reuses the scratch array.
+  auto drain = [st](rt_status s) {
+    cudaStreamSynchronize(st);
+    return s;
+  };
+  constexpr uint32_t kNonFinite = 0x100u;
   if (h.nsegs &&
       cudaMemcpyAsync(dsegs, h.segs, sizeof(Seg) * h.nsegs, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return RT_ERR_CUDA;
+    return drain(RT_ERR_CUDA);
   if (cudaMemcpyAsync(dleaves, h.leaves, sizeof(Leaf) * h.nleaves, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return RT_ERR_CUDA;
+    return drain(RT_ERR_CUDA);
   // The error word survives from earlier calls: clear it.
-  if (cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 4, st) != cudaSuccess) return RT_ERR_CUDA;
+  if (cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 4, st) != cudaSuccess) return drain(RT_ERR_CUDA);
+  // Non-finite vertices are rejected before any sort runs: the sort replay
+  // assumes keys that IEEE `<` orders totally.
+  k_check_finite<<<(n + 255) / 256, 256, 0, st>>>(d_triangles, n, ctr + 2, kNonFinite);
+  if (cudaGetLastError() != cudaSuccess) return drain(RT_ERR_CUDA);
+  if (cudaMemcpyAsync(h.flags, ctr, sizeof(h.flags), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return drain(RT_ERR_CUDA);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return RT_ERR_CUDA;
+  if (h.flags[2] & kNonFinite) return RT_ERR_INVALID_SCENE;
   k_iota<<<(n + 255) / 256, 256, 0, st>>>(idx, n);
   for (uint32_t L = 0; L < h.levels; L++) {
     uint32_t s0 = h.level_off[L], s1 = h.level_off[L + 1];
@@ -725,7 +763,7 @@ extern "C" rt_status rtBuildBvhNoAlloc(const rt_triangle *d_triangles, uint32_t 
     if (ns == 0) continue;
     const Seg *ls = dsegs + s0;
     // Queue count and head start at zero for every level; keep the error word.
-    if (cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 2, st) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 2, st) != cudaSuccess) return drain(RT_ERR_CUDA);
     k_keys<<<(n + 255) / 256, 256, 0, st>>>(ls, ns, d_triangles, idx, key, n);
     k_enqueue<<<(ns + 255) / 256, 256, 0, st>>>(ls, ns, queue, ctr);
     uint32_t maxn = 0;
@@ -738,8 +776,9 @@ extern "C" rt_status rtBuildBvhNoAlloc(const rt_triangle *d_triangles, uint32_t 
     uint32_t s0 = h.level_off[L], s1 = h.level_off[L + 1];
     if (s1 > s0) k_inner<<<(s1 - s0 + 255) / 256, 256, 0, st>>>(dsegs + s0, s1 - s0, d_nodes);
   }
-  if (cudaGetLastError() != cudaSuccess) return RT_ERR_CUDA;
-  if (cudaMemcpyAsync(h.flags, ctr, sizeof(h.flags), cudaMemcpyDeviceToHost, st) != cudaSuccess) return RT_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return drain(RT_ERR_CUDA);
+  if (cudaMemcpyAsync(h.flags, ctr, sizeof(h.flags), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return drain(RT_ERR_CUDA);
   if (cudaStreamSynchronize(st) != cudaSuccess) return RT_ERR_CUDA;
   return h.flags[2] ? RT_ERR_INTERNAL : RT_SUCCESS;
 }

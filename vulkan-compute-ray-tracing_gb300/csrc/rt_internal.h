@@ -152,6 +152,7 @@ inline bool use_wavefront(const RenderOpts &o, const rt_render_params &p) {
 // Tree used when a scene is uploaded without nodes (rtSetTuning "bvh.builder").
 struct BuildOpts {
   int builder = 0;  // 0 the reference's Bvh.h tree (bit-exact), 1 LBVH, 2 PLOC
+  int test_error_level = -1;  // test hook of gpu_build_bvh's error word (-1: off)
 };
 
 // One job of a batched render (render.cu: k_render_batch).
@@ -174,8 +175,12 @@ cudaError_t launch_batch_advance(BatchJob *d_jobs, uint32_t n_jobs, cudaStream_t
 // ---------------------------------------------------------------- bvh_build.cu
 // Builds the Bvh.h node array on the GPU. `axes` holds rand() % 3 for every
 // node in pop order (2*n - 1 values, host-generated from glibc's rand()).
+// test_error_level >= 0 (a test hook, "bvh.test_error_level") records an
+// error bit after that level's sort, as an overflow would; the build must
+// then fail with RT_ERR_INTERNAL.
 rt_status gpu_build_bvh(const rt_triangle *d_tris, uint32_t n, const uint8_t *h_axes, rt_bvh_node *d_nodes,
-                        cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen);
+                        cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen,
+                        int test_error_level = -1);
 
 // ---------------------------------------------------------------- export.cu
 cudaError_t launch_export(const float *in, uint32_t n, float gamma, uint8_t *out, cudaStream_t st);
