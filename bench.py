@@ -1,6 +1,6 @@
-"""Benchmark: closest-hit ray casting on the 1.31M-triangle displaced icosphere.
+"""Benchmark of the ray-trace hot path on one GB300.
 
-Workload (one step): the two ray batches of the closest-hit configuration,
+Headline (one step): the two ray batches of the closest-hit configuration,
 traced against the mesh through the C ABI —
   * coherent: 4,194,304 primary rays of a 2048x2048 pinhole at (0,0,-3)
     looking +z, vfov 40 degrees;
@@ -9,21 +9,31 @@ traced against the mesh through the C ABI —
 The mesh is the icosahedron subdivided 8 times (1,310,720 triangles), radius
 1, vertices displaced radially by 0.05*N(0,1); its BVH is built on the GPU
 node-for-node as the reference's Bvh.h builds it. All inputs are seeded
-synthetic data.
+synthetic data (no public dataset is involved).
 
-Reported:
+Reported on the one JSON line:
   value      rays/s (Mrays/s) with rays resident in HBM (device API);
   e2e        the same through the host-array entry point (rtTraceClosestHost),
              pinned host rays in and hits out inside the timed region;
-  roofline   algorithmic bytes of the culled traversal of the reference tree
-             (48 B per node or triangle record fetched + 32 B ray + 16 B hit,
-             counted by the oracle) / CUDA-event time of the trace kernel,
-             against the measured HBM copy bandwidth;
-  cpu_baseline  the oracle (fp32, culled traversal, OpenMP) on a bounded
-             sample of the same rays, on this machine's host cores.
-`--impl reference` times the reference path's CPU implementation (the
-oracle restatement of the shader's hit_bvh; the reference's own GLSL needs a
-Vulkan stack that is not available) on the same workload.
+  roofline   the dominant casting kernel: algorithmic bytes of the culled
+             traversal of the reference tree (48 B per node or triangle
+             record + 32 B ray + 16 B hit, counted by the oracle) over its
+             live time against the measured HBM copy bandwidth, plus the
+             physical DRAM and issue-slot fractions from the committed ncu
+             capture;
+  parity     every ray's hit index against the oracle, the tie fraction and
+             the largest t/u/v error against the fp64 oracle;
+  cpu_baseline  the oracle (fp32, culled traversal, OpenMP) on every ray,
+             on this machine's host cores, with the reference's own
+             single-threaded Bvh::createBvh time;
+  render_configs  the render-side configurations: Cornell 256^2 frames,
+             the 8M-triangle 1080p progressive render (64 frames), the
+             256-scene batch against one request per launch, and served
+             Poisson requests against one request at a time (p50/p99), each
+             with its own end-to-end figure.
+`--impl reference` times the reference path's CPU implementation (its own
+compute shader's hit_bvh, compiled from source; the GLSL itself needs a
+Vulkan stack that is not available) on every ray of the same workload.
 """
 from __future__ import annotations
 
@@ -43,9 +53,9 @@ import numpy as np  # noqa: E402
 METRIC = "Mrays/s incl. secondary (1 GB300, hit-exact); served renders/s + p50/p99 vs plain"
 WORKLOAD = "closest-hit, icosphere L8 (1,310,720 tris), 4,194,304 coherent + 4,194,304 incoherent rays"
 # Algorithmic bytes per ray (oracle, culled near-first traversal of the
-# reference tree over 1/16 of each batch): 48 * (nodes + triangles) + 48.
-ALG_BYTES_COHERENT = 48.0 * (531.24 + 61.47) + 48.0
-ALG_BYTES_INCOHERENT = 48.0 * (369.86 + 41.28) + 48.0
+# reference tree over every ray of each batch): 48 * (nodes + triangles) + 48.
+ALG_BYTES_COHERENT = 48.0 * (530.158 + 61.469) + 48.0
+ALG_BYTES_INCOHERENT = 48.0 * (370.590 + 41.355) + 48.0
 RAYS_PER_BATCH = 2048 * 2048
 
 
@@ -59,18 +69,24 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per trace launch from the committed ncu summary, if any."""
+def kernel_profiles():
+    """Per-kernel figures of the committed ncu capture of this workload
+    (profiles/trace_closest_icosphere_l8.md, lines "roofline_kernel: <name>
+    key=value ..."): DRAM bytes, warp instructions issued and the ncu
+    duration of one launch."""
     p = os.path.join(ROOT, "profiles", "trace_closest_icosphere_l8.md")
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip())
-            except ValueError:
-                return None
-    return None
+        if not line.startswith("roofline_kernel:"):
+            continue
+        parts = line.split(":", 1)[1].split()
+        try:
+            out[parts[0]] = {k: float(v) for k, v in (x.split("=", 1) for x in parts[1:])}
+        except ValueError:
+            continue
+    return out
 
 
 class ClockSampler:
@@ -147,10 +163,10 @@ def max_over_ranks(x: float, world: int) -> float:
     return replicas.max_over_ranks(x, world)
 
 
-def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 30.0):
-    """The oracle on a bounded sample of both batches, all host threads."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+def cpu_baseline(oracle, tris, coherent, incoherent, nodes, target_s: float = 30.0):
+    """The oracle's culled traversal (fp32, OpenMP, every host thread) on a
+    bounded sample of both batches — every ray when that fits in about
+    `target_s` seconds."""
     thr = oracle.max_threads()
     probe = 4096
     t0 = time.perf_counter()
@@ -165,65 +181,130 @@ def cpu_baseline(tris, coherent, incoherent, nodes, target_s: float = 30.0):
     oracle.trace(tris, nodes, b, slack=0.0)
     dt = time.perf_counter() - t0
     n = len(a) + len(b)
+    model = cpu_model()
     which = "every ray of both batches" if stride == 1 else f"one ray in {stride} of each batch"
-    return {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": thr, "kind": "port",
-            "sample": f"{which} ({n} rays), oracle fp32 culled traversal, {thr} OpenMP threads, {dt:.1f} s"}
+    return {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": thr, "kind": "port", "cpu_model": model,
+            "sample": f"{which} ({n} rays), oracle fp32 culled traversal, {thr} OpenMP threads on {model}, "
+                      f"{dt:.1f} s"}
+
+
+def parity_block(oracle, tris, nodes, batches):
+    """Every ray's closest-hit index against the fp32 oracle (rays whose two
+    nearest candidates lie within 1e-6 relative t are ties and excluded),
+    and t, u, v against the fp64 oracle on one ray in 16 where both pick the
+    same triangle. `batches` is [(rays, gpu_hits)]."""
+    rays_n = mism = ties_n = f64_n = f64_agree = 0
+    err = [0.0, 0.0, 0.0]
+    for rays, got in batches:
+        want, st = oracle.trace(tris, nodes, rays, stats=True)
+        ties = (st[:, 2] & 1) != 0
+        gi, wi = got.view(np.int32)[:, 0], want.view(np.int32)[:, 0]
+        rays_n += len(rays)
+        ties_n += int(ties.sum())
+        mism += int(((gi != wi) & ~ties).sum())
+        sub = np.arange(0, len(rays), 16)
+        tri64, tuv = oracle.trace_f64(tris, nodes, rays[sub])
+        gs = got[sub]
+        gsi = gs.view(np.int32)[:, 0]
+        agree = (gsi == tri64) & (gsi >= 0)
+        f64_n += int((gsi >= 0).sum())
+        f64_agree += int(agree.sum())
+        for c in range(3):
+            ref = tuv[agree, c]
+            rel = np.abs(gs[agree, 1 + c].astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-30)
+            if len(rel):
+                err[c] = max(err[c], float(rel.max()))
+    return {"rays": rays_n, "index_mismatch_outside_ties": mism, "tie_fraction": ties_n / max(rays_n, 1),
+            "max_rel_err_t": err[0], "max_rel_err_u": err[1], "max_rel_err_v": err[2],
+            "fp64_sample": f"one ray in 16 ({rays_n // 16} rays); {f64_agree} of {f64_n} GPU hits pick the fp64 "
+                           f"oracle's triangle",
+            "bar": "index bit-exact outside ties; t, u, v within 1e-5 relative of fp64"}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def reference_bvh(oracle, tris):
+    """The reference tree, built by the reference's own Bvh::createBvh where
+    it was compiled from its source (single thread, timed), else by the
+    oracle's restatement (equal node for node). Returns (nodes, seconds,
+    what)."""
+    t0 = time.perf_counter()
+    if oracle.ref_available():
+        nodes = oracle.ref_build_bvh(tris, 1)
+        what = "the reference's Bvh::createBvh (src/ray-tracing/Bvh.h, compiled from source), one thread"
+    else:
+        nodes = oracle.build_bvh(tris, 1)[0]
+        what = "the oracle's restatement of Bvh::createBvh, one thread"
+    return nodes, time.perf_counter() - t0, what
 
 
 def run_reference(args):
-    """--impl reference: the reference path's CPU implementation, timed."""
-    world, rank, _ = dist_init()
-    if rank != 0:
+    """--impl reference: the reference path's CPU implementation, timed on
+    this machine's host cores over every ray of both batches per step. Its
+    inputs come from the oracle's restatement of the seeded generators (byte
+    for byte the product's), so nothing of the product is loaded."""
+    if int(os.environ.get("RANK", "0")) != 0:
         return
-    import rtgb
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    tris, mats, coherent, incoherent = make_workload(rtgb)
-    nodes, _ = oracle.build_bvh(tris, 1)
+    tris, coherent, incoherent = oracle.closest_hit_workload()
+    nodes, build_s, build_what = reference_bvh(oracle, tris)
     thr = oracle.max_threads()
     # The reference's own traversal where its shader was compiled from source
     # (oracle/_ref: hit_bvh of ray-trace-compute.comp, 16-entry stack), else
-    # the oracle's restatement of it.
+    # the oracle's literal restatement of the same loop.
     if oracle.ref_shader_available():
-        kind, what = "reference", "the reference shader's own hit_bvh (compiled from ray-trace-compute.comp)"
+        kind, what = "reference", "the reference shader's own hit_bvh (ray-trace-compute.comp compiled from source)"
 
         def cast(rays):
             return oracle.ref_shader_trace(tris, nodes, rays)
     else:
-        kind, what = "port", "oracle restatement of hit_bvh (culled)"
+        kind, what = "port", "the oracle's literal restatement of hit_bvh (16-entry stack, no t-culling)"
 
         def cast(rays):
-            return oracle.trace(tris, nodes, rays, slack=0.0)
-    # Each step: a fixed sample of both batches sized to ~4 s of CPU work.
-    probe = 4096
-    t0 = time.perf_counter()
-    cast(coherent[::1024][:probe // 2])
-    cast(incoherent[::1024][:probe // 2])
-    rate = probe / max(time.perf_counter() - t0, 1e-6)
-    per_batch = int(min(RAYS_PER_BATCH, max(2048, rate * 4.0 / 2)))
-    stride = max(1, RAYS_PER_BATCH // per_batch)
-    a, b = coherent[::stride][:per_batch], incoherent[::stride][:per_batch]
+            return oracle.trace(tris, nodes, rays, mode=1, stack_size=16, slack=0.0)
+    warm = np.concatenate([coherent[::128], incoherent[::128]])
     for _ in range(args.warmup):
-        cast(a[:256])
+        cast(warm)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cast(a)
-        cast(b)
+        cast(coherent)
+        cast(incoherent)
     dt = time.perf_counter() - t0
-    n = (len(a) + len(b)) * args.steps
+    n = 2 * RAYS_PER_BATCH * args.steps
     value = n / dt / 1e6
+    model = cpu_model()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_per_step": f"one ray in {stride} of each batch "
-                                                            f"({len(a) + len(b)} rays)"},
-        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": thr, "kind": kind,
-                         "sample": f"one ray in {stride} of each batch, {what}, {thr} OpenMP threads"},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "rays_per_step": 2 * RAYS_PER_BATCH,
+                   "warmup_sample": f"{len(warm)} rays (one in 128 of each batch) per warm-up step"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": thr, "kind": kind, "cpu_model": model,
+                         "sample": f"every ray of both batches ({2 * RAYS_PER_BATCH} per step), {what}, "
+                                   f"{thr} OpenMP threads on {model}"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference GLSL path unavailable on this box (no graphics stack); " +
-                ("its own source, rewritten into C++, runs on the host cores" if kind == "reference"
-                 else "its CPU restatement is timed"),
+        "bvh_build_reference": {"seconds": build_s, "what": build_what},
+        "note": "the reference's GLSL path is unavailable on this box (no graphics stack); " +
+                ("its own source, rewritten into C++, runs on the host cores; its 16-entry stack truncates, "
+                 "as in the reference" if kind == "reference" else "its CPU restatement is timed"),
     }
     print(json.dumps(line), flush=True)
 
@@ -276,11 +357,26 @@ def run_gpu(args):
     value = rays_step * args.steps * world / (ms_max / 1e3) / 1e6
     kern = [[ev[k][b][0].elapsed_time(ev[k][b][1]) for k in range(args.steps)] for b in range(2)]
     coh_ms, inc_ms = statistics.mean(kern[0]), statistics.mean(kern[1])
-    alg = [ALG_BYTES_COHERENT * RAYS_PER_BATCH, ALG_BYTES_INCOHERENT * RAYS_PER_BATCH]
-    # Average algorithmic bytes per launch / average launch duration (GB/s).
-    achieved = ((alg[0] + alg[1]) / 2) / (((coh_ms + inc_ms) / 2) / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    traffic = traffic_from_profile()
+    prof = kernel_profiles()
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+
+    def kernel_roofline(name, batch_ms, alg_bytes_per_ray, sm_mhz):
+        # Algorithmic bytes of one batch over the batch's live CUDA-event time
+        # (the cast is ~97% of it; the rest is ray reordering); the ncu
+        # capture's DRAM bytes and issued warp instructions of the same
+        # kernel over the same live time give the physical fractions.
+        achieved = alg_bytes_per_ray * RAYS_PER_BATCH / (batch_ms / 1e3) / 1e9
+        e = {"kernel": name, "batch_ms": batch_ms, "achieved": achieved, "frac": achieved / peak,
+             "alg_bytes_per_ray": alg_bytes_per_ray}
+        p = prof.get(name)
+        if p:
+            e["traffic"] = p["dram_bytes"]
+            e["dram_bytes_per_ray"] = p["dram_bytes"] / RAYS_PER_BATCH
+            e["dram_frac"] = p["dram_bytes"] / (batch_ms / 1e3) / (peak * 1e9)
+            e["issue_frac"] = p["inst_issued"] / (batch_ms / 1e3 * sm_mhz * 1e6 * nsm * 4)
+            e["ncu_duration_ms"] = p["duration_ms"]
+        return e
 
     # End to end: host arrays (pinned) through rtTraceClosestHost.
     h_rays = [torch.from_numpy(coherent).pin_memory(), torch.from_numpy(incoherent).pin_memory()]
@@ -301,11 +397,26 @@ def run_gpu(args):
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_value = rays_step * args.steps * world / e2e_s / 1e6
     # Sanity: the e2e hits equal the device-path hits.
-    same = all(torch.equal(h_hits[b].view(torch.int32), d_hits[b].cpu().view(torch.int32)) for b in range(2))
+    gpu_hits = [d_hits[b].cpu().numpy() for b in range(2)]
+    same = all(np.array_equal(h_hits[b].numpy().view(np.int32), gpu_hits[b].view(np.int32)) for b in range(2))
 
     if rank != 0:
         ctx.close()
         return
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    per = [kernel_roofline("k_trace_packets", coh_ms, ALG_BYTES_COHERENT, sm_mhz),
+           kernel_roofline("k_trace_wide", inc_ms, ALG_BYTES_INCOHERENT, sm_mhz)]
+    dom = max(per, key=lambda e: e["batch_ms"])
+    roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["achieved"], "peak": peak, "unit": "GB/s",
+                "frac": dom["frac"], "traffic": dom.get("traffic"), "peak_kind": peak_kind,
+                "dram_frac": dom.get("dram_frac"), "issue_frac": dom.get("issue_frac"),
+                "note": "achieved/frac: the oracle's algorithmic bytes (48 B per node or triangle record of the "
+                        "culled traversal of the reference tree, + 48 B ray and hit) over the live time; "
+                        "frac > 1 is L1/L2 reuse. dram_frac: the ncu capture's DRAM bytes over the live time "
+                        "against the HBM peak; issue_frac: its issued warp instructions over 4 issue slots per SM "
+                        "per cycle at the sampled SM clock — the bound these kernels meet",
+                "per_kernel": {e["kernel"]: e for e in per}}
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -315,19 +426,14 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}", "coherent_grays": RAYS_PER_BATCH / coh_ms / 1e6,
                    "incoherent_grays": RAYS_PER_BATCH / inc_ms / 1e6, "bvh_build_ms": info.build_ms,
                    "bvh_depth": info.depth},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind,
-                     # DRAM bytes per ray actually moved (ncu), beside the
-                     # algorithmic bytes: frac > 1 is L1/L2 reuse.
-                     "dram_bytes_per_ray": traffic / RAYS_PER_BATCH if traffic else None,
-                     "alg_bytes_per_ray": {"coherent": ALG_BYTES_COHERENT, "incoherent": ALG_BYTES_INCOHERENT}},
+        "roofline": roofline,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_step * 32,
                 "d2h_bytes_per_step": rays_step * 16, "matches_device_path": bool(same)},
         # Per batch: 7 reordering kernels (extent, histogram, 3-kernel scan,
         # scatter, init) + 2 casting kernels (packets, then the listed
         # chunks per lane); two batches per step.
         "gpu_launches": 18 * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     # Separately reported: the same workload on trees that are not the
     # reference's (1 a linear BVH, 2 agglomerative clustering); the hits are
@@ -351,8 +457,27 @@ def run_gpu(args):
         line[key] = alt
         sc_l.release()
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(tris, coherent, incoherent, sc.bvh())
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        # The reference tree from the reference's own builder (one thread,
+        # timed); the GPU's tree must equal it node for node.
+        ref_nodes, build_s, build_what = reference_bvh(oracle, tris)
+        cols = [0, 1, 2, 4, 5, 6, 7, 8, 9]
+        line["config"]["bvh_equals_reference"] = bool(
+            np.array_equal(sc.bvh().view(np.uint32)[:, cols], ref_nodes.view(np.uint32)[:, cols]))
+        line["cpu_baseline"] = cpu_baseline(oracle, tris, coherent, incoherent, ref_nodes)
+        line["cpu_baseline"]["bvh_build_reference_s"] = build_s
+        line["cpu_baseline"]["bvh_build_reference"] = build_what
+        line["parity"] = parity_block(oracle, tris, ref_nodes,
+                                      [(coherent, gpu_hits[0]), (incoherent, gpu_hits[1])])
     ctx.close()
+    if world == 1 and not args.closest_hit_only:
+        # The rest of the metric (Mrays/s including secondary rays; served
+        # renders/s with p50/p99 against the plain form), one key per
+        # configuration, each with its own end-to-end figure.
+        del d_rays, d_hits, h_rays, h_hits
+        torch.cuda.empty_cache()
+        line["render_configs"] = render_configs(args)
     print(json.dumps(line), flush=True)
 
 
@@ -364,112 +489,179 @@ def _line(workload, metric, value, unit, args, extra):
     print(json.dumps(d), flush=True)
 
 
-def run_render(args):
-    """Config 0: Cornell box + 12,000 soup triangles, 256x256, 1 spp, 8 bounces."""
+def _timed(stream, fn, reps):
+    """CUDA-event milliseconds of `reps` calls of fn on `stream`."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(reps):
+        fn(k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def render_c0(ctx, steps: int, warmup: int):
+    """Cornell box + 12,000 soup triangles, 256x256, 1 spp, 8 bounces: one
+    progressive frame per step (the reference's per-frame dispatch)."""
     import torch
     import rtgb
-    ctx = rtgb.Context(0)
-    t, m, s = rtgb.gen_cornell(1, 12000, 0)
+    t, m, _ = rtgb.gen_cornell(1, 12000, 0)
     sc = ctx.upload_scene(t, m)
     W = H = 256
     sc.set_camera(rtgb.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H))
     stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
     acc = torch.zeros((H, W, 4), device="cuda")
     host = torch.empty((H, W, 4)).pin_memory()
-    for k in range(args.warmup):
-        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=stream.cuda_stream)
+    for k in range(warmup):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=sp)
     torch.cuda.synchronize()
     ctx.segments(reset=True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for k in range(args.steps):
-        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=args.warmup + k, stream=stream.cuda_stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = _timed(stream, lambda k: sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=warmup + k, stream=sp),
+                steps)
     seg = ctx.segments(reset=True)
+    # End to end: the same frames through rtRender, each image read back to
+    # pinned host memory inside the timed region.
     t0 = time.perf_counter()
-    for k in range(args.steps):
-        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=stream.cuda_stream)
+    for k in range(steps):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=sp)
         host.copy_(acc, non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     seg2 = ctx.segments(reset=True)
-    _line("render 256x256 1spp 8 bounces, Cornell box + 12,000 soup triangles", METRIC, seg / (ms / 1e3) / 1e6,
-          "Mrays/s", args, {"ms_per_step": ms / args.steps, "segments_per_step": seg / args.steps,
-                            "e2e": {"value": seg2 / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
-                                    "d2h_bytes_per_step": W * H * 16}})
-    ctx.close()
+    sc.release()
+    return {"workload": "render 256x256, 1 spp per frame, 8 bounces, Cornell box + 12,000 soup triangles",
+            "value": seg / (ms / 1e3) / 1e6, "unit": "Mrays/s", "frames": steps, "ms_per_frame": ms / steps,
+            "segments_per_frame": seg / steps,
+            "e2e": {"value": seg2 / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 16}}
 
 
-def run_batch(args):
-    """Config 2: many scenes of uneven size, batched launch vs one launch per render."""
+def large_c4(ctx, frames: int):
+    """~8M triangles (6x6 grid of flattened displaced level-7 icospheres +
+    the Cornell box), 1920x1080, `frames` progressive frames of 1 spp, 8
+    bounces."""
+    import torch
+    import rtgb
+    t, m = rtgb.gen_grid(4, 6, 6, 7, 0.35, 0.05, 222222, 3.0)
+    sc = ctx.upload_scene(t, m)
+    info = sc.info()
+    W, H = 1920, 1080
+    sc.set_camera(rtgb.camera_look_at([0, 2, -40], [0, -6, 0], [0, 1, 0], 40.0, W, H))
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    acc = torch.zeros((H, W, 4), device="cuda")
+    host = torch.empty((H, W, 4)).pin_memory()
+    sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=0, stream=sp)
+    torch.cuda.synchronize()
+    ctx.segments(reset=True)
+    ms = _timed(stream, lambda k: sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=sp), frames)
+    seg = ctx.segments(reset=True)
+    # End to end: the final image of the progressive run read back.
+    t0 = time.perf_counter()
+    for k in range(frames):
+        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=sp)
+    host.copy_(acc, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    seg2 = ctx.segments(reset=True)
+    sc.release()
+    return {"workload": f"progressive render 1920x1080, {frames} frames x 1 spp, 8 bounces, "
+                        f"{info.triangles} triangles (6x6 flattened displaced level-7 icospheres + Cornell box)",
+            "value": seg / (ms / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_frame": ms / frames,
+            "bvh_build_ms": info.build_ms, "bvh_depth": info.depth, "triangles": info.triangles,
+            "e2e": {"value": seg2 / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 16 // frames}}
+
+
+def batch_c2(ctx, n_scenes: int, reps: int):
+    """256 scenes of uneven size, 4 spp, 8 bounces: the batched launch (one
+    persistent launch over the small jobs plus wavefront side streams, and
+    its CUDA-graph replay) against one request per launch."""
     import torch
     import rtgb
     from rtgb import workloads as wl
-    ctx = rtgb.Context(0)
-    specs = wl.batch_scene_specs(args.batch_scenes)
+    specs = wl.batch_scene_specs(n_scenes)
     scenes, jobs, accs = [], [], []
     t0 = time.perf_counter()
     build_ms = 0.0
     tris_total = 0
-    for sp in specs:
-        t, m, s = wl.make_scene(sp)
+    for sp_ in specs:
+        t, m, s = wl.make_scene(sp_)
         sc = ctx.upload_scene(t, m, spheres=s)
         build_ms += sc.info().build_ms
         tris_total += len(t)
         scenes.append(sc)
-        acc = torch.zeros((sp.side, sp.side, 4), device="cuda")
+        acc = torch.zeros((sp_.side, sp_.side, 4), device="cuda")
         accs.append(acc)
-        jobs.append(rtgb.make_job(sc, wl.default_camera(sp.side), acc, sp.side, sp.side, 4, 8))
+        jobs.append(rtgb.make_job(sc, wl.default_camera(sp_.side), acc, sp_.side, sp_.side, 4, 8))
     setup_s = time.perf_counter() - t0
     stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
+    for sc, sp_ in zip(scenes, specs):
+        sc.set_camera(wl.default_camera(sp_.side))
 
-    def plain():
-        for sc, sp, acc in zip(scenes, specs, accs):
-            sc.set_camera(wl.default_camera(sp.side))
-            sc.render(acc, sp.side, sp.side, spp=4, max_bounces=8, stream=sptr)
+    def plain(_k):
+        for sc, sp_, acc in zip(scenes, specs, accs):
+            sc.render(acc, sp_.side, sp_.side, spp=4, max_bounces=8, stream=sptr)
 
     b = ctx.batch(jobs)
+    old_mode = ctx.get_tuning("render.mode")
     res = {}
-    for name, fn in (("plain", plain), ("batched", lambda: b.launch(sptr)), ("batched_graph", lambda: b.launch_graph(sptr))):
-        fn()  # warm-up
+
+    def one_launch(k):
+        ctx.set_tuning("render.mode", 0)
+        plain(k)
+
+    for name, fn in (("plain_one_launch", one_launch), ("plain", plain), ("batched", lambda k: b.launch(sptr)),
+                     ("batched_graph", lambda k: b.launch_graph(sptr))):
+        fn(0)  # warm-up
         torch.cuda.synchronize()
         ctx.segments(reset=True)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        seg = ctx.segments(reset=True) / args.steps
+        ms = _timed(stream, fn, reps) / reps
+        ctx.set_tuning("render.mode", old_mode)
+        seg = ctx.segments(reset=True) / reps
         res[name] = {"ms_per_batch": ms, "mrays_s": seg / (ms / 1e3) / 1e6, "renders_s": len(jobs) / (ms / 1e3)}
+    # End to end: the graph replay plus every image read back to pinned host.
+    hosts = [torch.empty_like(a, device="cpu").pin_memory() for a in accs]
+    d2h = sum(a.numel() * 4 for a in accs)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        b.launch_graph(sptr)
+        with torch.cuda.stream(stream):
+            for h, a in zip(hosts, accs):
+                h.copy_(a, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / reps
     b.destroy()
-    _line(f"batched render: {len(jobs)} scenes ({tris_total} triangles), sides 128-1024, 4 spp, 8 bounces",
-          METRIC, res["batched_graph"]["mrays_s"], "Mrays/s", args,
-          {"modes": res, "speedup_vs_plain": res["batched_graph"]["renders_s"] / res["plain"]["renders_s"],
-           "setup_s": setup_s, "bvh_build_ms_total": build_ms})
-    ctx.close()
+    for sc in scenes:
+        sc.release()
+    best = res["batched_graph"]
+    return {"workload": f"batched render: {len(jobs)} scenes ({tris_total} triangles), sides 128-1024, 4 spp, "
+                        f"8 bounces", "value": best["renders_s"], "unit": "renders/s", "mrays_s": best["mrays_s"],
+            "modes": res, "speedup_vs_one_launch_per_request": best["renders_s"] / res["plain_one_launch"]["renders_s"],
+            "speedup_vs_rtrender_per_request": best["renders_s"] / res["plain"]["renders_s"],
+            "plain_forms": "plain_one_launch: one k_render launch per request, the reference's one dispatch per "
+                           "frame; plain: rtRender per request (megakernel below 2^20 pixels, wavefront above)",
+            "setup_s": setup_s, "bvh_build_ms_total": build_ms, "reps": reps,
+            "e2e": {"value": len(jobs) / e2e_s, "unit": "renders/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": d2h}}
 
 
-def run_serve(args):
-    """Config 3: open-loop Poisson requests over resident scenes; continuous
-    batching vs one request per launch."""
-    import rtgb
+def serve_c3(ctx, n_scenes: int, n_requests: int, rates, sides=(256, 512, 1024), spp_max: int = 64,
+             max_active: int = 64, spp_step: int = 4):
+    """Open-loop Poisson requests over resident scenes: continuous batching
+    against one request at a time, p50/p99 latency beside renders/s. Every
+    request's image is copied back to host memory (end to end)."""
     from rtgb import serve
     from rtgb import workloads as wl
-    ctx = rtgb.Context(0)
-    specs = wl.batch_scene_specs(args.serve_scenes, base_seed=2000)
-    datas = [wl.make_scene(sp) for sp in specs]
-    sides = tuple(int(x) for x in args.serve_sides.split(","))
+    specs = wl.batch_scene_specs(n_scenes, base_seed=2000)
+    datas = [wl.make_scene(sp_) for sp_ in specs]
     out = {}
-    for rate in [float(x) for x in args.serve_rates.split(",")]:
-        reqs = wl.request_stream(args.serve_requests, rate, len(specs), sides=sides, spp_max=args.serve_spp_max)
-        for mode, kw in (("continuous", dict(max_active=args.serve_active, spp_per_step=args.serve_step)),
+    for rate in rates:
+        reqs = wl.request_stream(n_requests, rate, len(specs), sides=sides, spp_max=spp_max)
+        for mode, kw in (("continuous", dict(max_active=max_active, spp_per_step=spp_step)),
                          ("plain", dict(max_active=1, spp_per_step=0))):
             with serve.Server(ctx, hbm_budget_bytes=150 << 30, **kw) as srv:
                 handles = [srv.add_scene(*d) for d in datas]
@@ -477,49 +669,75 @@ def run_serve(args):
                 for w in warm:
                     srv.wait(w)
                 srv.reset_stats()
-                wall, ids = wl.run_stream(srv, handles, reqs)
+                wall, ids = wl.run_stream(srv, handles, reqs, keep_image=True)
                 st = srv.stats()
                 out[f"{mode}@{rate:g}"] = {"renders_s": len(reqs) / wall, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
                                            "mean_ms": st.mean_ms, "steps": st.steps, "wall_s": wall,
                                            "uploads": st.scene_uploads, "evictions": st.scene_evictions}
+    ratios = {f"{r:g}": out[f"continuous@{r:g}"]["renders_s"] / out[f"plain@{r:g}"]["renders_s"] for r in rates}
     best = max(v["renders_s"] for k, v in out.items() if k.startswith("continuous"))
-    _line(f"served renders: {args.serve_requests} Poisson requests per rate over {len(specs)} resident scenes, "
-          f"sides {sides}, spp 1-{args.serve_spp_max}, 8 bounces", METRIC, best, "renders/s", args,
-          {"rates": out})
+    return {"workload": f"served renders: {n_requests} Poisson requests per rate over {len(specs)} resident "
+                        f"scenes, sides {tuple(sides)}, spp 1-{spp_max}, 8 bounces, 150 GB budget",
+            "value": best, "unit": "renders/s", "rates": out, "speedup_vs_plain": ratios,
+            "e2e": {"value": best, "unit": "renders/s",
+                    "note": "requests submitted from the host with each image copied back to host memory; "
+                            "wall clock from the first arrival to the last completion"}}
+
+
+def run_render(args):
+    import rtgb
+    ctx = rtgb.Context(0)
+    r = render_c0(ctx, args.steps, args.warmup)
+    _line(r.pop("workload"), METRIC, r.pop("value"), r.pop("unit"), args, r)
+    ctx.close()
+
+
+def run_batch(args):
+    import rtgb
+    ctx = rtgb.Context(0)
+    r = batch_c2(ctx, args.batch_scenes, max(1, args.steps))
+    _line(r.pop("workload"), METRIC, r.pop("value"), r.pop("unit"), args, r)
+    ctx.close()
+
+
+def run_serve(args):
+    import rtgb
+    ctx = rtgb.Context(0)
+    r = serve_c3(ctx, args.serve_scenes, args.serve_requests, [float(x) for x in args.serve_rates.split(",")],
+                 tuple(int(x) for x in args.serve_sides.split(",")), args.serve_spp_max, args.serve_active,
+                 args.serve_step)
+    _line(r.pop("workload"), METRIC, r.pop("value"), r.pop("unit"), args, r)
     ctx.close()
 
 
 def run_large(args):
-    """Config 4: ~8M triangles (6x6 grid of flattened displaced level-7
-    icospheres + the Cornell box), 1920x1080, 1 spp per frame, 8 bounces."""
-    import torch
     import rtgb
     ctx = rtgb.Context(0)
-    t, m = rtgb.gen_grid(4, 6, 6, 7, 0.35, 0.05, 222222, 3.0)
-    sc = ctx.upload_scene(t, m)
-    info = sc.info()
-    W, H = 1920, 1080
-    sc.set_camera(rtgb.camera_look_at([0, 2, -40], [0, -6, 0], [0, 1, 0], 40.0, W, H))
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    acc = torch.zeros((H, W, 4), device="cuda")
-    frames = args.steps
-    sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=0, stream=stream.cuda_stream)
-    torch.cuda.synchronize()
-    ctx.segments(reset=True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for k in range(frames):
-        sc.render(acc, W, H, spp=1, max_bounces=8, sample_index=k, stream=stream.cuda_stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    seg = ctx.segments(reset=True)
-    _line(f"progressive render 1920x1080, {frames} frames x 1 spp, 8 bounces, {info.triangles} triangles",
-          METRIC, seg / (ms / 1e3) / 1e6, "Mrays/s", args,
-          {"ms_per_frame": ms / frames, "bvh_build_ms": info.build_ms, "bvh_depth": info.depth,
-           "triangles": info.triangles})
+    r = large_c4(ctx, args.steps)
+    _line(r.pop("workload"), METRIC, r.pop("value"), r.pop("unit"), args, r)
     ctx.close()
+
+
+def render_configs(args):
+    """The render-side configurations, reported as keys of the default line."""
+    import rtgb
+    out = {}
+    ctx = rtgb.Context(0)
+    try:
+        for key, fn in (("render_cornell_256", lambda: render_c0(ctx, 20, 3)),
+                        ("progressive_8m_1080p", lambda: large_c4(ctx, 64)),
+                        ("batched_256_scenes", lambda: batch_c2(ctx, args.batch_scenes, 1)),
+                        ("served_poisson", lambda: serve_c3(ctx, args.serve_scenes, args.serve_requests,
+                                                             [float(x) for x in args.serve_rates.split(",")],
+                                                             tuple(int(x) for x in args.serve_sides.split(",")),
+                                                             args.serve_spp_max, args.serve_active,
+                                                             args.serve_step))):
+            t0 = time.perf_counter()
+            out[key] = fn()
+            out[key]["wall_s"] = time.perf_counter() - t0
+    finally:
+        ctx.close()
+    return out
 
 
 def main():
@@ -529,11 +747,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--closest-hit-only", action="store_true",
+                    help="skip the render, batched, served and large-scene configurations of the default line")
     ap.add_argument("--workload", default="closest-hit", choices=["closest-hit", "render", "batch", "serve", "large"])
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--serve-scenes", type=int, default=64)
-    ap.add_argument("--serve-requests", type=int, default=60)
-    ap.add_argument("--serve-rates", default="1,4,64")
+    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-rates", default="10,100,2000")
     ap.add_argument("--serve-sides", default="256,512,1024")
     ap.add_argument("--serve-spp-max", type=int, default=64)
     ap.add_argument("--serve-active", type=int, default=64)

@@ -46,6 +46,11 @@ def _load():
         "oracle_max_threads": (I32, []),
         "oracle_wide_fold": (I32, [P, U32, U32, P, P, P, ctypes.POINTER(U32), ctypes.POINTER(U32)]),
         "oracle_trace_wide": (I32, [P, U32, P, U32, I32, P, P, U32, P, P, I32]),
+        "oracle_gen_icosphere": (U32, [ctypes.c_uint64, U32, ctypes.c_float, ctypes.c_float, U32, P]),
+        "oracle_camera_look_at": (I32, [P, P, P, ctypes.c_float, U32, U32, P]),
+        "oracle_gen_camera_rays": (None, [P, U32, U32, ctypes.c_float, ctypes.c_float, P]),
+        "oracle_gen_random_rays": (None, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_float, P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -367,3 +372,47 @@ def denoise(img: np.ndarray, sigma: float = 2.0, ksigma: float = 2.0, threshold:
 
 def max_threads() -> int:
     return LIB.oracle_max_threads()
+
+
+# ------------------------------------------------------------------ workloads
+# The seeded inputs of the closest-hit measurement (oracle/workloads.cpp),
+# byte-equal to the product library's generators, so that the reference arm
+# of the bench makes its inputs without the product library.
+
+def gen_icosphere(seed: int, level: int, radius: float = 1.0, sigma: float = 0.05, material: int = 0):
+    n = LIB.oracle_gen_icosphere(seed, level, radius, sigma, material, None)
+    out = np.zeros((n, 12), np.float32)
+    LIB.oracle_gen_icosphere(seed, level, radius, sigma, material, _p(out))
+    return out
+
+
+def camera_look_at(eye, target, up, vfov_deg: float, width: int, height: int) -> np.ndarray:
+    """12 floats: origin, lower-left, horizontal, vertical."""
+    e, t, u = (np.ascontiguousarray(x, np.float32) for x in (eye, target, up))
+    cam = np.zeros(12, np.float32)
+    if not LIB.oracle_camera_look_at(_p(e), _p(t), _p(u), vfov_deg, width, height, _p(cam)):
+        raise ValueError("degenerate camera")
+    return cam
+
+
+def gen_camera_rays(cam: np.ndarray, width: int, height: int, tmin: float = 1e-4, tmax: float = 1e4):
+    cam = np.ascontiguousarray(cam, np.float32).reshape(12)
+    rays = np.zeros((width * height, 8), np.float32)
+    LIB.oracle_gen_camera_rays(_p(cam), width, height, tmin, tmax, _p(rays))
+    return rays
+
+
+def gen_random_rays(seed: int, n: int, lo: float = -1.5, hi: float = 1.5, tmin: float = 1e-4, tmax: float = 1e4):
+    rays = np.zeros((n, 8), np.float32)
+    LIB.oracle_gen_random_rays(seed, n, lo, hi, tmin, tmax, _p(rays))
+    return rays
+
+
+def closest_hit_workload(side: int = 2048, level: int = 8):
+    """The closest-hit measurement's inputs: the displaced icosphere (seed 1,
+    radius 1, sigma 0.05), side x side primary rays of a pinhole at
+    (0, 0, -3) looking at the origin with a 40 degree field of view, and
+    side^2 random rays (seed 3, origins in [-1.5, 1.5]^3)."""
+    tris = gen_icosphere(1, level)
+    cam = camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, side, side)
+    return tris, gen_camera_rays(cam, side, side), gen_random_rays(3, side * side)

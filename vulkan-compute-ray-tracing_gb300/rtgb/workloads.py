@@ -77,9 +77,10 @@ def request_stream(n: int, rate_hz: float, n_scenes: int, seed: int = 77, sides=
     return out
 
 
-def run_stream(server, handles, reqs, bounces: int = 8):
-    """Submits requests at their arrival times (open loop) and waits for all.
-    Returns (wall seconds from first arrival to last completion, ids)."""
+def run_stream(server, handles, reqs, bounces: int = 8, keep_image: bool = False):
+    """Submits requests at their arrival times (open loop) and waits for all;
+    with keep_image every result is copied back to host memory. Returns
+    (wall seconds from first arrival to last completion, ids)."""
     ids = [None] * len(reqs)
     t0 = time.perf_counter()
 
@@ -89,7 +90,7 @@ def run_stream(server, handles, reqs, bounces: int = 8):
             if delay > 0:
                 time.sleep(delay)
             cam = default_camera(r.side, r.jitter_seed)
-            ids[i] = server.submit(handles[r.scene], cam, r.side, r.side, r.spp, bounces, keep_image=False)
+            ids[i] = server.submit(handles[r.scene], cam, r.side, r.side, r.spp, bounces, keep_image=keep_image)
 
     th = threading.Thread(target=feeder)
     th.start()
