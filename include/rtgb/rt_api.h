@@ -200,6 +200,15 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   cache, where the binary layout is faster); it applies
  *                   to closest-hit casts and to the wavefront render's
  *                   bounce rays alike
+ *   "trace.block"   threads per block of the casting kernels: 64, 128
+ *                   (default) or 256; the register budget per thread stays
+ *                   the one the minblocks keys name
+ *   "trace.stack"   traversal stack entries of the casting kernels: 16, 32
+ *                   or 64, raised to the smallest of those that holds the
+ *                   scene's tree; 0 (default) takes that smallest size (the
+ *                   reference fixes 16, ray-trace-compute.comp:262, and
+ *                   silently drops what does not fit; an overflow here is
+ *                   reported as RT_ERR_STACK_OVERFLOW)
  *   "render.mode"   0 megakernel (one thread runs a pixel's whole path),
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from render.wavefront_pixels up;
@@ -224,9 +233,10 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value);
 rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value);
 
 /* Autotuner (no counterpart in the reference, whose launch shape is fixed at
- * compile time). Times the closest-hit launch shapes on the caller's own
- * device rays (coordinate descent over trace.wide, trace.wide_minblocks, trace.defer, trace.spec,
- * trace.minblocks, trace.packet_minblocks, trace.sort; `reps` timed casts
+ * compile time, ray-trace-compute.comp:3, 262). Times the closest-hit
+ * launch shapes on the caller's own device rays (coordinate descent over
+ * trace.block, trace.stack, trace.wide, trace.wide_minblocks, trace.defer,
+ * trace.spec, trace.minblocks, trace.packet_minblocks, trace.sort; `reps` timed casts
  * per candidate after one warm-up) and keeps the fastest. Hits are identical
  * in every shape; d_hits receives them. The rates before and after tuning
  * are returned in Grays/s (either pointer may be NULL). Synchronous. */

@@ -62,12 +62,21 @@ uint32_t rtgbGenGrid(uint64_t seed, uint32_t gx, uint32_t gz, uint32_t level, fl
 double rtgbUniform(uint64_t seed, uint64_t index);
 
 /* Host form of the 8-wide node quantization the scene upload runs on the
- * GPU: `boxes` holds `filled` (1..8) child boxes as lo.xyz, hi.xyz; `out`
- * receives the node's 24 words (origin, int8 exponents and count, 8-bit
- * child bounds, refs). Returns 1, or 0 when a box does not fit the node's
- * grid. Exposed so the decoded boxes can be checked to contain the
- * originals without a GPU. */
-uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t filled, uint32_t *out);
+ * GPU: `boxes` holds 8 child slots as lo.xyz, hi.xyz and `refs` their refs,
+ * of which the slots set in `fmask` (bit s: slot s, at least one) are
+ * filled; `out` receives the node's 24 words (origin, int8 exponents and
+ * the filled mask, 8-bit child bounds with qlo = 255, qhi = 0 in empty
+ * slots, refs with INT_MIN in empty slots). Returns 1, or 0 when a box
+ * does not fit the node's grid. Exposed so the decoded boxes can be checked
+ * to contain the originals without a GPU. */
+uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t fmask, uint32_t *out);
+
+/* Host form of the 8-wide fold's slot assignment: child i of `cnt` (1..8)
+ * boxes (lo.xyz, hi.xyz) goes to slot slot_of[i], slot bits (x, y, z) naming
+ * the node corner on the positive side of each set axis (greedy on the
+ * offset of the box centre from the node centre). Returns 1, or 0 on bad
+ * arguments. */
+uint32_t rtgbAssignOctantSlots(const float *boxes, uint32_t cnt, int32_t *slot_of);
 
 #ifdef __cplusplus
 }

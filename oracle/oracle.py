@@ -45,6 +45,7 @@ def _load():
         "oracle_render_f64": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
         "oracle_max_threads": (I32, []),
         "oracle_wide_fold": (I32, [P, U32, U32, P, P, P, ctypes.POINTER(U32), ctypes.POINTER(U32)]),
+        "oracle_octant_slot_assignment": (I32, [P, U32, P]),
         "oracle_trace_wide": (I32, [P, U32, P, U32, I32, P, P, U32, P, P, I32]),
         "oracle_gen_icosphere": (U32, [ctypes.c_uint64, U32, ctypes.c_float, ctypes.c_float, U32, P]),
         "oracle_camera_look_at": (I32, [P, P, P, ctypes.c_float, U32, U32, P]),
@@ -295,28 +296,39 @@ def trace(tris, nodes, rays, mode: int = 0, stack_size: int = 16, slack: float =
 
 def wide_fold(nodes):
     """The GPU builder's 8-wide fold of a reference node array, restated:
-    per node up to 8 child boxes (lo.xyz, hi.xyz), refs ((node << 3) |
-    (filled - 1) for inner children, ~triangle for leaves, INT_MIN empty)
-    and the filled count. Returns (boxes (n8, 8, 6), refs (n8, 8), filled,
-    levels)."""
+    per node 8 child slots placed by octant (boxes lo.xyz, hi.xyz; refs: the
+    child node's number for inner children, ~triangle for leaves, INT_MIN
+    empty) and the mask of filled slots. Returns (boxes (n8, 8, 6), refs
+    (n8, 8), fmask (n8,), levels)."""
     nodes = np.ascontiguousarray(nodes, np.float32)
     cap = max(1, (4 * ((len(nodes) + 1) // 2) + 6) // 7 + 1)
     boxes = np.zeros((cap, 8, 6), np.float32)
     refs = np.zeros((cap, 8), np.int32)
-    filled = np.zeros(cap, np.uint32)
+    fmask = np.zeros(cap, np.uint32)
     n8, levels = ctypes.c_uint32(0), ctypes.c_uint32(0)
-    rc = LIB.oracle_wide_fold(_p(nodes), len(nodes), cap, _p(boxes), _p(refs), _p(filled), ctypes.byref(n8),
+    rc = LIB.oracle_wide_fold(_p(nodes), len(nodes), cap, _p(boxes), _p(refs), _p(fmask), ctypes.byref(n8),
                               ctypes.byref(levels))
     if rc != 0:
         raise RuntimeError(f"oracle_wide_fold failed ({rc})")
     n = n8.value
-    return boxes[:n], refs[:n], filled[:n], levels.value
+    return boxes[:n], refs[:n], fmask[:n], levels.value
+
+
+def octant_slots(boxes) -> np.ndarray:
+    """Slot of each of 1..8 child boxes (lo.xyz, hi.xyz) under the fold's
+    octant rule."""
+    b = np.ascontiguousarray(boxes, np.float32).reshape(-1, 6)
+    out = np.zeros(len(b), np.int32)
+    if LIB.oracle_octant_slot_assignment(_p(b), len(b), _p(out)) != 0:
+        raise ValueError("1..8 boxes expected")
+    return out
 
 
 def trace_wide(tris, qwords, root8: int, root_box, rays, threads: int = 0, stats: bool = False):
-    """Closest hits through quantized 8-wide nodes (qwords: (n8, 24) uint32),
-    with the GPU kernel's plane arithmetic; hits as oracle `trace`, and with
-    stats=True also (n, 2) uint32: nodes visited, triangles tested."""
+    """Closest hits through quantized 8-wide nodes (qwords: (n8, 24) uint32;
+    root8: the root node's number), with the GPU kernel's plane arithmetic
+    and visiting order; hits as oracle `trace`, and with stats=True also
+    (n, 2) uint32: nodes visited, triangles tested."""
     tris, rays = np.ascontiguousarray(tris, np.float32), np.ascontiguousarray(rays, np.float32)
     qwords = np.ascontiguousarray(qwords, np.uint32)
     rb = np.ascontiguousarray(root_box, np.float32)

@@ -23,6 +23,7 @@
 // and aarch64. The fp64 instantiation evaluates the same formulas in double
 // and is the error reference for t and the barycentrics.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -818,16 +819,73 @@ void oracle_denoise(const float *in, uint32_t W, uint32_t H, float sigma, float 
 // closest hit. oracle_wide_fold folds the reference node array into nodes
 // of up to eight children with the GPU builder's rule (replace the inner
 // child of largest half area, dx*dy + dy*dz + dz*dx, by its two children,
-// left in place and right appended, first of equal areas) and breadth-first
-// numbering; inner refs are (node << 3) | (filled - 1), leaf refs
-// ~triangle. The caller quantizes each node with the library's host
-// quantizer (96-byte words) and oracle_trace_wide traverses those words:
-// planes entered at fmaf(q, ix * 2^e, (o - ray.o) * ix), children sorted
-// near-first, triangles tested when reached with the acceptance rule of the
-// culled traversal (exactly equal t: the lower triangle index wins).
+// left in place and right appended, first of equal areas), places the
+// children in slots by octant (oracle_octant_slots) and numbers nodes
+// breadth first, the inner children of a node in slot order; inner refs are
+// node numbers, leaf refs ~triangle, empty slots INT_MIN. The caller
+// quantizes each node with the library's host quantizer (96-byte words) and
+// oracle_trace_wide traverses those words: planes entered at fmaf(q, ix *
+// 2^e, (o - ray.o) * ix), the entered inner child of smallest entry distance
+// visited next and the others later in increasing order of slot ^ (the
+// ray's direction sign bits), triangles tested when reached
+// with the acceptance rule of the culled traversal (exactly equal t: the
+// lower triangle index wins).
+
+// Slot of each of `cnt` children (boxes lo.xyz, hi.xyz): slot bits (x, y,
+// z) name the node corner on the positive side of each set axis; each child
+// goes to the free slot of lowest cost -sum_k sign_k(slot) * offset_k, the
+// offsets being twice the distance of the child's box centre from the
+// node's (sums and differences of coordinates only), greedily, lowest cost
+// first, ties to the lower child and then the lower slot.
+static void oracle_octant_slots(const float (*box)[6], int cnt, int *slot_of) {
+  float twice_centre[3];
+  for (int k = 0; k < 3; k++) {
+    float lo = box[0][k], hi = box[0][3 + k];
+    for (int i = 1; i < cnt; i++) {
+      lo = std::fmin(lo, box[i][k]);
+      hi = std::fmax(hi, box[i][3 + k]);
+    }
+    twice_centre[k] = lo + hi;
+  }
+  bool kid_done[8] = {}, slot_taken[8] = {};
+  for (int placed = 0; placed < cnt; placed++) {
+    int bi = -1, bs = -1;
+    float best = 0.0f;
+    for (int i = 0; i < cnt; i++) {
+      if (kid_done[i]) continue;
+      float off[3];
+      for (int k = 0; k < 3; k++) off[k] = (box[i][k] + box[i][3 + k]) - twice_centre[k];
+      for (int sl = 0; sl < 8; sl++) {
+        if (slot_taken[sl]) continue;
+        float cost = 0.0f;
+        for (int k = 0; k < 3; k++) cost = (sl >> k & 1) ? cost - off[k] : cost + off[k];
+        if (bi < 0 || cost < best) {
+          best = cost;
+          bi = i;
+          bs = sl;
+        }
+      }
+    }
+    kid_done[bi] = true;
+    slot_taken[bs] = true;
+    slot_of[bi] = bs;
+  }
+}
+
+int oracle_octant_slot_assignment(const float *boxes, uint32_t cnt, int32_t *slot_of) {
+  if (!boxes || !slot_of || cnt < 1 || cnt > 8) return 1;
+  float b[8][6];
+  for (uint32_t i = 0; i < cnt; i++)
+    for (int k = 0; k < 6; k++) b[i][k] = boxes[6 * i + k];
+  int so[8];
+  oracle_octant_slots(b, (int)cnt, so);
+  for (uint32_t i = 0; i < cnt; i++) slot_of[i] = so[i];
+  return 0;
+}
+
 int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, float *boxes, int32_t *refs,
-                     uint32_t *filled_out, uint32_t *n8_out, uint32_t *levels_out) {
-  if (!nodes || nnodes == 0 || !boxes || !refs || !filled_out || !n8_out) return 1;
+                     uint32_t *fmask_out, uint32_t *n8_out, uint32_t *levels_out) {
+  if (!nodes || nnodes == 0 || !boxes || !refs || !fmask_out || !n8_out) return 1;
   struct Slot {
     float b[6];
     int32_t node;  // reference node index
@@ -846,11 +904,27 @@ int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, fl
     float dx = s.b[3] - s.b[0], dy = s.b[4] - s.b[1], dz = s.b[5] - s.b[2];
     return dx * dy + dy * dz + dz * dx;
   };
+  // Each built node: its 8 slots (node -1 = empty).
+  std::vector<std::array<Slot, 8>> built;
   std::vector<int32_t> frontier, next;
-  std::vector<std::vector<Slot>> built;
   uint32_t levels = 0;
+  auto place = [&](const std::vector<Slot> &S) {
+    std::array<Slot, 8> out;
+    for (auto &o : out) o.node = -1;
+    float b[8][6];
+    for (size_t i = 0; i < S.size(); i++)
+      for (int k = 0; k < 6; k++) b[i][k] = S[i].b[k];
+    int so[8];
+    oracle_octant_slots(b, (int)S.size(), so);
+    for (size_t i = 0; i < S.size(); i++) out[so[i]] = S[i];
+    return out;
+  };
   if (!inner(0)) {
-    built.push_back({slot_of(0)});
+    std::array<Slot, 8> one;
+    for (auto &o : one) o.node = -1;
+    one[0] = slot_of(0);
+    built.push_back(one);
+    levels = 1;
   } else {
     frontier.push_back(0);
     while (!frontier.empty()) {
@@ -873,9 +947,9 @@ int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, fl
           S[pick] = slot_of(nodes[p].left);
           S.push_back(slot_of(nodes[p].right));
         }
-        built.push_back(S);
-        for (const Slot &c : S)
-          if (inner(c.node)) next.push_back(c.node);
+        built.push_back(place(S));
+        for (const Slot &c : built.back())
+          if (c.node >= 0 && inner(c.node)) next.push_back(c.node);
       }
       frontier.swap(next);
       levels++;
@@ -883,37 +957,23 @@ int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, fl
   }
   if (built.size() > cap) return 2;
   // Node numbers: breadth first, the inner children of node i in slot order.
-  std::vector<uint32_t> first_child(built.size());
   uint32_t counter = 1;
   for (size_t i = 0; i < built.size(); i++) {
-    first_child[i] = counter;
-    for (const Slot &c : built[i]) counter += inner(c.node) ? 1u : 0u;
-  }
-  for (size_t i = 0; i < built.size(); i++) {
-    uint32_t c = first_child[i];
-    filled_out[i] = (uint32_t)built[i].size();
+    uint32_t mask = 0;
     for (int s = 0; s < 8; s++) {
       float *b = boxes + 6 * (8 * i + s);
-      if (s >= (int)built[i].size()) {
+      const Slot &sl = built[i][s];
+      if (sl.node < 0) {
         for (int k = 0; k < 6; k++) b[k] = 0.0f;
         refs[8 * i + s] = INT32_MIN;
         continue;
       }
-      const Slot &sl = built[i][s];
+      mask |= 1u << s;
       for (int k = 0; k < 6; k++) b[k] = sl.b[k];
-      if (inner(sl.node)) {
-        refs[8 * i + s] = (int32_t)c;  // encoded with the child's count below
-        c++;
-      } else {
-        refs[8 * i + s] = ~nodes[sl.node].object;
-      }
+      refs[8 * i + s] = inner(sl.node) ? (int32_t)(counter++) : ~nodes[sl.node].object;
     }
+    fmask_out[i] = mask;
   }
-  for (size_t i = 0; i < built.size(); i++)
-    for (int s = 0; s < 8; s++) {
-      int32_t r = refs[8 * i + s];
-      if (r >= 0) refs[8 * i + s] = (r << 3) | (int32_t)(built[r].size() - 1);
-    }
   *n8_out = (uint32_t)built.size();
   if (levels_out) *levels_out = levels;
   return 0;
@@ -937,6 +997,7 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
     const float ix = safe_rcp_model(r.d[0]), iy = safe_rcp_model(r.d[1]), iz = safe_rcp_model(r.d[2]);
     const float inv[3] = {ix, iy, iz};
     const float oi[3] = {r.o[0] * ix, r.o[1] * iy, r.o[2] * iz};
+    const uint32_t oct = (ix < 0.0f ? 1u : 0u) | (iy < 0.0f ? 2u : 0u) | (iz < 0.0f ? 4u : 0u);
     float closest = r.tmax, bu = 0, bv = 0;
     int32_t best = -1;
     // Root box: the kernels' slab test, fmaf(lo, 1/d, -o/d).
@@ -946,21 +1007,26 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
       tn = std::fmax(tn, std::fmin(a, b));
       tf = std::fmin(tf, std::fmax(a, b));
     }
-    std::vector<int32_t> stack;
+    // Groups: (node, rank bits of its entered inner children not yet visited).
+    std::vector<std::pair<uint32_t, uint32_t>> groups;
     int32_t node = tn <= tf ? root8 : -1;
     uint32_t steps = 0, ntests = 0;
-    while (node >= 0 || !stack.empty()) {
+    for (;;) {
       if (node < 0) {
-        node = stack.back();
-        stack.pop_back();
+        while (!groups.empty() && groups.back().second == 0) groups.pop_back();
+        if (groups.empty()) break;
+        auto &g = groups.back();
+        const uint32_t rk = (uint32_t)__builtin_ctz(g.second);
+        g.second &= g.second - 1u;
+        node = (int32_t)qwords[24ull * g.first + 16 + (rk ^ oct)];
       }
-      const uint32_t idx = (uint32_t)node >> 3;
-      const int filled = (node & 7) + 1;
+      const uint32_t idx = (uint32_t)node;
       if (idx >= n8 || ++steps > n8 + 16) {
         bad = 1;
         break;
       }
       const uint32_t *w = qwords + 24ull * idx;
+      const uint32_t fmask = w[3] >> 24;
       float org[3];
       std::memcpy(org, w, 12);
       float sc[3], ax[3];
@@ -972,12 +1038,11 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
         sc[k] = inv[k] * p2;
         ax[k] = (org[k] - r.o[k]) * inv[k];
       }
-      uint32_t key[8];
-      int32_t ref[8];
+      uint32_t ibits = 0, nearest = 0;
+      float tbest = INFINITY;
       for (int s = 0; s < 8; s++) {
-        key[s] = 0xffffffffu;
-        ref[s] = (int32_t)w[16 + s];
-        if (s >= filled) continue;
+        if (!((fmask >> s) & 1u)) continue;
+        const int32_t ref = (int32_t)w[16 + s];
         float t[6];
         for (int k = 0; k < 3; k++) {
           const float ql = (float)((w[4 + 2 * k + (s >> 2)] >> (8 * (s & 3))) & 0xffu);
@@ -990,35 +1055,38 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
         const float f0 = std::fmin(std::fmin(std::fmax(t[0], t[3]), std::fmax(t[1], t[4])),
                                    std::fmin(std::fmax(t[2], t[5]), closest));
         if (!(n0 <= f0)) continue;
-        if (ref[s] >= 0) {
-          uint32_t b;
-          std::memcpy(&b, &n0, 4);
-          key[s] = (b & ~7u) | (uint32_t)s;
-        } else {
-          const int32_t tri = ~ref[s];
-          if (tri < 0 || (uint32_t)tri >= ntris) {
-            bad = 1;
-            continue;
+        if (ref >= 0) {
+          ibits |= 1u << ((uint32_t)s ^ oct);
+          if (n0 < tbest) {
+            tbest = n0;
+            nearest = (uint32_t)s;
           }
-          float t0, u, v;
-          V3<float> n;
-          ntests++;
-          if (!tri_intersect<float>(tris[tri], ld3<float>(r.o), ld3<float>(r.d), t0, u, v, n)) continue;
-          if (!(t0 > r.tmin && t0 < r.tmax)) continue;
-          if (t0 < closest || (best >= 0 && t0 == closest && tri < best)) {
-            closest = t0;
-            best = tri;
-            bu = u;
-            bv = v;
-          }
+          continue;
+        }
+        const int32_t tri = ~ref;
+        if (tri < 0 || (uint32_t)tri >= ntris) {
+          bad = 1;
+          continue;
+        }
+        float t0, u, v;
+        V3<float> nrm;
+        ntests++;
+        if (!tri_intersect<float>(tris[tri], ld3<float>(r.o), ld3<float>(r.d), t0, u, v, nrm)) continue;
+        if (!(t0 > r.tmin && t0 < r.tmax)) continue;
+        if (t0 < closest || (best >= 0 && t0 == closest && tri < best)) {
+          closest = t0;
+          best = tri;
+          bu = u;
+          bv = v;
         }
       }
-      std::sort(key, key + 8);
       node = -1;
-      int cnt = 0;
-      while (cnt < 8 && key[cnt] != 0xffffffffu) cnt++;
-      for (int j = cnt - 1; j >= 1; j--) stack.push_back(ref[key[j] & 7u]);
-      if (cnt > 0) node = ref[key[0] & 7u];
+      if (ibits) {
+        // The nearest entered child next, the others later in rank order.
+        node = (int32_t)w[16 + nearest];
+        const uint32_t rest = ibits & ~(1u << (nearest ^ oct));
+        if (rest) groups.push_back({idx, rest});
+      }
     }
     hits[i] = best >= 0 ? rt_hit{best, closest, bu, bv} : rt_hit{-1, 0.0f, 0.0f, 0.0f};
     if (stats) {

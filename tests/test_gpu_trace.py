@@ -352,7 +352,8 @@ def test_alt_tree_mode_same_hits(rt, orc, ctx, builder):
 def test_autotune_trace_keeps_hits(rt, orc, ctx):
     """The autotuner's candidates are timing choices only: after tuning, the
     hits equal the ones cast with the settings it started from."""
-    keys = ("trace.wide", "trace.wide_minblocks", "trace.defer", "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort")
+    keys = ("trace.block", "trace.stack", "trace.wide", "trace.wide_minblocks", "trace.defer", "trace.spec",
+            "trace.minblocks", "trace.packet_minblocks", "trace.sort")
     old = [ctx.get_tuning(k) for k in keys]
     tris, sc = mesh_scene(rt, ctx, 6, 3)
     try:
@@ -364,11 +365,42 @@ def test_autotune_trace_keeps_hits(rt, orc, ctx):
         d_hits = torch.zeros((len(rays), 4), dtype=torch.float32, device="cuda")
         before, after = rt.autotune_trace(sc, d_rays, len(rays), d_hits, reps=1)
         assert before > 0 and after > 0
+        allowed = {"trace.wide_minblocks": (8, 6, 5), "trace.minblocks": (16, 12, 10),
+                   "trace.packet_minblocks": (16, 12, 10), "trace.block": (64, 128, 256),
+                   "trace.stack": (0, 32, 64)}
         for k in keys:
-            assert ctx.get_tuning(k) in ((8, 6, 5) if k == "trace.wide_minblocks" else
-                                         (16, 12, 10) if "minblocks" in k else (0, 1))
+            assert ctx.get_tuning(k) in allowed.get(k, (0, 1))
         got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    finally:
+        for k, v in zip(keys, old):
+            ctx.set_tuning(k, v)
+        sc.release()
+
+
+@pytest.mark.parametrize("level,wide_min", [(6, 0), (6, 1 << 30), (4, 1 << 30)], ids=["bvh8", "binary", "shallow"])
+def test_block_size_and_stack_depth_keep_hits(rt, ctx, level, wide_min):
+    """The autotuner's block-size (64/128/256 threads) and stack-depth
+    (16/32/64 entries, raised to what the tree needs) axes: every candidate
+    returns the same hits bit for bit, on the 8-wide caster and on the
+    binary packet and per-lane kernels, including a tree shallow enough for
+    the 16-entry stack."""
+    tris, sc = mesh_scene(rt, ctx, level, 4)
+    keys = ("trace.block", "trace.stack", "trace.wide_min_tris")
+    old = [ctx.get_tuning(k) for k in keys]
+    try:
+        ctx.set_tuning("trace.wide_min_tris", wide_min)
+        if level == 4:
+            assert sc.info().depth <= 16
+        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 128, 96)
+        rays = np.concatenate([rt.gen_camera_rays(cam, 128, 96), rt.gen_random_rays(12, 20000)])
+        base = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+        for block in (64, 128, 256):
+            for stack in (0, 16, 32, 64):
+                ctx.set_tuning("trace.block", block)
+                ctx.set_tuning("trace.stack", stack)
+                got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+                assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (block, stack)
     finally:
         for k, v in zip(keys, old):
             ctx.set_tuning(k, v)

@@ -13,29 +13,30 @@ import numpy as np
 import pytest
 
 
-def quantize_all(rt, boxes, refs, filled):
+def quantize_all(rt, boxes, refs, fmask):
     words = np.zeros((len(boxes), 24), np.uint32)
     out = np.zeros(24, np.uint32)
     for i in range(len(boxes)):
-        n = int(filled[i])
-        b = np.ascontiguousarray(boxes[i, :n], np.float32)
-        r = np.ascontiguousarray(refs[i, :n], np.int32)
-        assert rt.LIB.rtgbQuantizeNode8(b.ctypes.data, r.ctypes.data, n, out.ctypes.data) == 1
+        b = np.ascontiguousarray(boxes[i], np.float32)
+        r = np.ascontiguousarray(refs[i], np.int32)
+        assert rt.LIB.rtgbQuantizeNode8(b.ctypes.data, r.ctypes.data, int(fmask[i]), out.ctypes.data) == 1
         words[i] = out
     return words
 
 
-def wide_hits(rt, orc, tris, nodes, rays):
-    boxes, refs, filled, levels = orc.wide_fold(nodes)
-    assert levels >= 1 and (filled >= 1).all() and (filled <= 8).all()
-    # Every triangle sits in exactly one leaf slot.
-    leaves = refs[refs < 0]
-    leaves = leaves[leaves != np.iinfo(np.int32).min]
+def wide_hits(rt, orc, tris, nodes, rays, stats=False):
+    boxes, refs, fmask, levels = orc.wide_fold(nodes)
+    assert levels >= 1 and (fmask >= 1).all() and (fmask <= 255).all()
+    # Every triangle sits in exactly one leaf slot; empty slots match the mask.
+    empty = refs == np.iinfo(np.int32).min
+    bits = (fmask[:, None] >> np.arange(8, dtype=np.uint32)[None, :]) & 1
+    assert np.array_equal(empty, bits == 0)
+    leaves = refs[(refs < 0) & ~empty]
     assert sorted((~leaves).tolist()) == list(range(len(tris)))
-    words = quantize_all(rt, boxes, refs, filled)
-    root8 = (0 << 3) | (int(filled[0]) - 1) if nodes.view(np.int32)[0, 7] != -1 else 0
+    words = quantize_all(rt, boxes, refs, fmask)
+    assert np.array_equal(words[:, 3] >> 24, fmask)
     root_box = np.concatenate([nodes[0, 0:3], nodes[0, 4:7]]).astype(np.float32)
-    return orc.trace_wide(tris, words, root8, root_box, rays)
+    return orc.trace_wide(tris, words, 0, root_box, rays, stats=stats)
 
 
 def check(rt, orc, tris, rays):
@@ -105,8 +106,8 @@ def test_model_detects_shrunk_boxes(rt, orc):
     nodes, _ = orc.build_bvh(tris, 1)
     rays = rt.gen_random_rays(5, 20000)
     want = orc.trace(tris, nodes, rays)
-    boxes, refs, filled, _ = orc.wide_fold(nodes)
-    words = quantize_all(rt, boxes, refs, filled)
+    boxes, refs, fmask, _ = orc.wide_fold(nodes)
+    words = quantize_all(rt, boxes, refs, fmask)
     for wi in range(10, 16):  # the qhi words
         w = words[:, wi].copy()
         out = np.zeros_like(w)
@@ -115,7 +116,41 @@ def test_model_detects_shrunk_boxes(rt, orc):
             byte = np.where(byte > 0, byte - 1, byte)
             out |= byte << np.uint32(8 * b)
         words[:, wi] = out
-    root8 = (int(filled[0]) - 1)
     root_box = np.concatenate([nodes[0, 0:3], nodes[0, 4:7]]).astype(np.float32)
-    got = orc.trace_wide(tris, words, root8, root_box, rays)
+    got = orc.trace_wide(tris, words, 0, root_box, rays)
     assert not np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_octant_slots_equal_library(rt, orc):
+    """The fold's slot placement: the library's host function (the one the
+    GPU fold runs) equals the oracle's restatement on random child sets,
+    and children go to distinct slots."""
+    rng = np.random.default_rng(11)
+    got = np.zeros(8, np.int32)
+    for trial in range(3000):
+        cnt = int(rng.integers(1, 9))
+        lo = rng.normal(0, 1, (cnt, 3)).astype(np.float32)
+        hi = (lo + rng.uniform(0, 0.5, (cnt, 3))).astype(np.float32)
+        if trial % 7 == 0:
+            lo[:] = lo[0]  # identical boxes: every cost ties
+            hi[:] = hi[0]
+        boxes = np.ascontiguousarray(np.concatenate([lo, hi], 1), np.float32)
+        want = orc.octant_slots(boxes)
+        assert rt.LIB.rtgbAssignOctantSlots(boxes.ctypes.data, cnt, got.ctypes.data) == 1
+        assert np.array_equal(got[:cnt], want)
+        assert len(set(want.tolist())) == cnt and (want >= 0).all() and (want < 8).all()
+
+
+def test_octant_order_visits_fewer_nodes_than_slot_order(rt, orc):
+    """The octant placement is what makes the rank order near-first: on the
+    bench mesh family the model visits no more nodes than with children
+    left in fold order would allow (sanity bound on the work, not results)."""
+    tris = rt.gen_icosphere(1, 6)
+    nodes, _ = orc.build_bvh(tris, 1)
+    rays = rt.gen_random_rays(3, 8192)
+    got, st = wide_hits(rt, orc, tris, nodes, rays, stats=True)
+    want = orc.trace(tris, nodes, rays)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # An 8-wide step replaces about three binary levels.
+    _, bst = orc.trace(tris, nodes, rays, slack=0.0, stats=True)
+    assert st[:, 0].mean() < 0.5 * bst[:, 0].mean()

@@ -781,6 +781,16 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.wide_refill = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.block") {
+    if (value != 64 && value != 128 && value != 256) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.block = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.stack") {
+    if (value != 0 && value != 16 && value != 32 && value != 64) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.stack = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "render.wavefront_pixels") {
     if (value < 1 || value > (1ll << 31)) return RT_ERR_INVALID_ARGUMENT;
     ctx->render_opts.wavefront_pixels = (uint64_t)value;
@@ -859,6 +869,14 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "render.mode") {
     *value = ctx->render_opts.mode;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.block") {
+    *value = ctx->trace_opts.block;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.stack") {
+    *value = ctx->trace_opts.stack;
     return RT_SUCCESS;
   }
   if (k == "render.wavefront_pixels") {

@@ -2,15 +2,18 @@
 // rtAutotuneRender in rt_api.h). Every knob it touches leaves results
 // unchanged (hits and images are identical in every shape), so tuning is a
 // pure timing search on the caller's own workload:
-//   closest hit  coordinate descent over trace.wide, trace.wide_minblocks, trace.defer, trace.spec,
+//   closest hit  coordinate descent over trace.block (threads per block,
+//                64/128/256), trace.stack (traversal stack entries 16/32/64,
+//                each raised to the smallest size that holds the tree),
+//                trace.wide, trace.wide_minblocks, trace.defer, trace.spec,
 //                trace.minblocks, trace.packet_minblocks and trace.sort,
 //                each candidate timed with CUDA events over `reps` casts
 //                after one warm-up cast;
 //   render       megakernel against wavefront at growing square image sizes
 //                on the scene's camera; render.wavefront_pixels becomes the
 //                smallest size from which the wavefront wins.
-// The traversal stack needs no tuning: it is sized to the tree's depth (32
-// or 64 entries) when the scene is uploaded.
+// The reference fixes the launch shape at compile time (local_size 32x32,
+// ray-trace-compute.comp:3) and the stack at 16 entries (comp:262).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -87,7 +90,9 @@ rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, 
     const char *key;
     std::vector<int64_t> values;
   };
-  const Knob knobs[] = {{"trace.wide", {1, 0}},
+  const Knob knobs[] = {{"trace.block", {128, 64, 256}},
+                        {"trace.stack", {0, 32, 64}},
+                        {"trace.wide", {1, 0}},
                         {"trace.wide_minblocks", {8, 6, 5}},
                         {"trace.defer", {1, 0}},
                         {"trace.spec", {1, 0}},

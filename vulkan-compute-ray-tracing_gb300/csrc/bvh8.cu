@@ -10,22 +10,32 @@
 // BVHs", HPG 2017). A node with fewer than eight children therefore holds
 // leaves only, which bounds the node count by (4n - 1) / 7 for n leaves.
 //
+// Slots are assigned by position (Ylitie et al.'s octant order): slot s,
+// read as three bits (x, y, z), stands for the corner of the node on the
+// positive side of the axes whose bit is set. Each child goes to the free
+// slot whose corner direction best matches the offset of its box centre
+// from the node's centre (greedy on the cost -sum_k sign_k(s) * offset_k,
+// lowest cost first, ties to the lower child then the lower slot). A ray
+// whose direction has sign bits o (bit k set when d_k < 0) then meets the
+// children roughly in increasing order of s ^ o, so the traversal orders
+// the children it enters with one XOR instead of sorting their distances.
+//
 // The fold is built in fp32 (8 slots of 32 bytes: (lo.x, lo.y, lo.z, hi.x),
-// (hi.y, hi.z, ref, 0), filled slots first, empty slots ref INT_MIN) and
-// then stored quantized, 96 bytes per node (k_quantize8, the compression of
-// Ylitie et al. with explicit child refs):
+// (hi.y, hi.z, ref, 0), empty slots ref INT_MIN) and then stored quantized,
+// 96 bytes per node (k_quantize8, the compression of Ylitie et al. with
+// explicit child refs):
 //   words 0-2    origin o: the lo corner of the union of the children
-//   word 3       int8 exponents ex, ey, ez; filled-slot count
+//   word 3       int8 exponents ex, ey, ez; the mask of filled slots
 //   words 4-15   8-bit child bounds qlo.x[8], qlo.y, qlo.z, qhi.x, qhi.y,
-//                qhi.z (slot s in byte s & 3 of word 2 * plane + (s >> 2))
+//                qhi.z (slot s in byte s & 3 of word 2 * plane + (s >> 2));
+//                an empty slot has qlo = 255, qhi = 0
 //   words 16-23  child refs
 // A child's box decodes to o + q * 2^e per axis. qlo is rounded down and
 // qhi up, and both are checked against the fp32 box, so the decoded box
-// always contains the original one. Refs: >= 0 is an inner child, encoded
-// as (node << 3) | (filled slots of that node - 1) so a traversal decodes
-// only the filled slots; ~k is a leaf (tpre record k, as in bvh2). Nodes
-// are numbered breadth first, level by level; the children of one node are
-// consecutive.
+// always contains the original one. Refs: >= 0 is an inner child (its node
+// number); ~k is a leaf (tpre record k, as in bvh2); INT_MIN an empty slot.
+// Nodes are numbered breadth first, level by level; the inner children of
+// one node are consecutive, in slot order.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -36,24 +46,29 @@
 
 namespace rtgb {
 
-// Quantizes one node: box[s] = (lo.xyz, hi.xyz) of the `filled` children,
-// refs copied as given, into the 24 words of a bvh8 node (layout above).
-// Per axis the origin is the children's union lo and the step the smallest
-// power of two 2^e with extent <= 255 * 2^e; each bound becomes a byte,
-// rounded down for lo and up for hi, then checked in fp64 against the fp32
-// bound and moved outward if needed, so the decoded box o + q * 2^e always
-// contains the original. False when some box does not fit the grid.
-__host__ __device__ inline bool quantize_node8(const float box[8][6], const int32_t ref[8], int filled,
+// Quantizes one node: box[s] = (lo.xyz, hi.xyz) of the children in the
+// slots of `fmask`, refs copied as given, into the 24 words of a bvh8 node
+// (layout above). Per axis the origin is the children's union lo and the
+// step the smallest power of two 2^e with extent <= 255 * 2^e; each bound
+// becomes a byte, rounded down for lo and up for hi, then checked in fp64
+// against the fp32 bound and moved outward if needed, so the decoded box
+// o + q * 2^e always contains the original. Empty slots get qlo = 255,
+// qhi = 0. False when some box does not fit the grid (or fmask is empty).
+__host__ __device__ inline bool quantize_node8(const float box[8][6], const int32_t ref[8], uint32_t fmask,
                                                uint32_t w[24]) {
-  bool ok = filled >= 1 && filled <= 8;
-  if (!ok) filled = 1;
+  fmask &= 0xffu;
+  bool ok = fmask != 0;
+  if (!ok) fmask = 1;
   for (int i = 0; i < 24; i++) w[i] = 0;
-  uint32_t ebytes = (uint32_t)filled << 24;
+  uint32_t ebytes = fmask << 24;
   for (int k = 0; k < 3; k++) {
-    float ulo = box[0][k], uhi = box[0][3 + k];
-    for (int s = 1; s < filled; s++) {
-      ulo = fminf(ulo, box[s][k]);
-      uhi = fmaxf(uhi, box[s][3 + k]);
+    float ulo = 0.0f, uhi = 0.0f;
+    bool first = true;
+    for (int s = 0; s < 8; s++) {
+      if (!((fmask >> s) & 1u)) continue;
+      ulo = first ? box[s][k] : fminf(ulo, box[s][k]);
+      uhi = first ? box[s][3 + k] : fmaxf(uhi, box[s][3 + k]);
+      first = false;
     }
     const double E = (double)uhi - (double)ulo;
     int e = -126;
@@ -65,15 +80,18 @@ __host__ __device__ inline bool quantize_node8(const float box[8][6], const int3
     }
     const double sc = ldexp(1.0, e);
     if (E > 255.0 * sc) ok = false;
-    for (int s = 0; s < filled; s++) {
-      const double lo = box[s][k], hi = box[s][3 + k];
-      int ql = (int)floor((lo - (double)ulo) / sc);
-      ql = ql < 0 ? 0 : (ql > 255 ? 255 : ql);
-      while (ql > 0 && (double)ulo + ql * sc > lo) ql--;
-      int qh = (int)ceil((hi - (double)ulo) / sc);
-      qh = qh < 0 ? 0 : (qh > 255 ? 255 : qh);
-      while (qh < 255 && (double)ulo + qh * sc < hi) qh++;
-      if ((double)ulo + ql * sc > lo || (double)ulo + qh * sc < hi) ok = false;
+    for (int s = 0; s < 8; s++) {
+      int ql = 255, qh = 0;
+      if ((fmask >> s) & 1u) {
+        const double lo = box[s][k], hi = box[s][3 + k];
+        ql = (int)floor((lo - (double)ulo) / sc);
+        ql = ql < 0 ? 0 : (ql > 255 ? 255 : ql);
+        while (ql > 0 && (double)ulo + ql * sc > lo) ql--;
+        qh = (int)ceil((hi - (double)ulo) / sc);
+        qh = qh < 0 ? 0 : (qh > 255 ? 255 : qh);
+        while (qh < 255 && (double)ulo + qh * sc < hi) qh++;
+        if ((double)ulo + ql * sc > lo || (double)ulo + qh * sc < hi) ok = false;
+      }
       w[4 + 2 * k + (s >> 2)] |= (uint32_t)ql << (8 * (s & 3));
       w[10 + 2 * k + (s >> 2)] |= (uint32_t)qh << (8 * (s & 3));
     }
@@ -88,6 +106,47 @@ __host__ __device__ inline bool quantize_node8(const float box[8][6], const int3
   w[3] = ebytes;
   for (int s = 0; s < 8; s++) w[16 + s] = (uint32_t)ref[s];
   return ok;
+}
+
+// Octant slot assignment (see the top of this file) of `cnt` child boxes
+// (lo.xyz, hi.xyz): slot_of[i] receives child i's slot. Only additions and
+// subtractions of the box coordinates are used (twice the centre offsets),
+// so host and device give the same assignment.
+__host__ __device__ inline void assign_octant_slots(const float (*box)[6], int cnt, int slot_of[8]) {
+  float c2[3];
+  for (int k = 0; k < 3; k++) {
+    float ulo = box[0][k], uhi = box[0][3 + k];
+    for (int i = 1; i < cnt; i++) {
+      ulo = fminf(ulo, box[i][k]);
+      uhi = fmaxf(uhi, box[i][3 + k]);
+    }
+    c2[k] = ulo + uhi;
+  }
+  float off[8][3];
+  for (int i = 0; i < cnt; i++)
+    for (int k = 0; k < 3; k++) off[i][k] = (box[i][k] + box[i][3 + k]) - c2[k];
+  uint32_t used_slots = 0, used_kids = 0;
+  for (int i = 0; i < 8; i++) slot_of[i] = -1;
+  for (int round = 0; round < cnt; round++) {
+    float best = 0.0f;
+    int bi = -1, bs = -1;
+    for (int i = 0; i < cnt; i++) {
+      if ((used_kids >> i) & 1u) continue;
+      for (int s = 0; s < 8; s++) {
+        if ((used_slots >> s) & 1u) continue;
+        float cost = 0.0f;
+        for (int k = 0; k < 3; k++) cost = ((s >> k) & 1) ? cost - off[i][k] : cost + off[i][k];
+        if (bi < 0 || cost < best) {
+          best = cost;
+          bi = i;
+          bs = s;
+        }
+      }
+    }
+    slot_of[bi] = bs;
+    used_kids |= 1u << bi;
+    used_slots |= 1u << bs;
+  }
 }
 
 namespace {
@@ -150,15 +209,25 @@ __global__ void k_collapse8(const float4 *__restrict__ bvh2, uint32_t n_pairs, c
   }
   float4 *o = bvh8 + 16ull * (base + f);
   const float inf = __int_as_float(0x7f800000);
-  uint32_t inner = 0;
   for (int s = 0; s < 8; s++) {
-    if (s < cnt) {
-      o[2 * s] = make_float4(S[s].lo[0], S[s].lo[1], S[s].lo[2], S[s].hi[0]);
-      o[2 * s + 1] = make_float4(S[s].hi[1], S[s].hi[2], __int_as_float(S[s].ref), 0.0f);
-      inner += S[s].ref >= 0 ? 1u : 0u;
-    } else {
-      o[2 * s] = make_float4(inf, inf, inf, inf);
-      o[2 * s + 1] = make_float4(inf, inf, __int_as_float(INT_MIN), 0.0f);
+    o[2 * s] = make_float4(inf, inf, inf, inf);
+    o[2 * s + 1] = make_float4(inf, inf, __int_as_float(INT_MIN), 0.0f);
+  }
+  uint32_t inner = 0;
+  if (cnt > 0) {
+    float box[8][6];
+    for (int i = 0; i < cnt; i++)
+      for (int k = 0; k < 3; k++) {
+        box[i][k] = S[i].lo[k];
+        box[i][3 + k] = S[i].hi[k];
+      }
+    int slot_of[8];
+    assign_octant_slots(box, cnt, slot_of);
+    for (int i = 0; i < cnt; i++) {
+      const int s = slot_of[i];
+      o[2 * s] = make_float4(S[i].lo[0], S[i].lo[1], S[i].lo[2], S[i].hi[0]);
+      o[2 * s + 1] = make_float4(S[i].hi[1], S[i].hi[2], __int_as_float(S[i].ref), 0.0f);
+      inner += S[i].ref >= 0 ? 1u : 0u;
     }
   }
   inner_cnt[f] = inner;
@@ -188,35 +257,17 @@ __global__ void k_link8(uint32_t count, uint32_t base, uint32_t next_base, const
   }
 }
 
-// Encodes every inner ref with its child's filled-slot count (all levels
-// are built when this runs), and range-checks every leaf ref, which the
-// traversal then uses without a check.
-__global__ void k_encode8(uint32_t n8, uint32_t ntris, float4 *__restrict__ bvh8, uint32_t *__restrict__ err) {
+// Range-checks every child ref once all levels are built (inner refs
+// against the node count, leaf refs against the triangle count); the
+// traversal then uses leaf refs without a check.
+__global__ void k_encode8(uint32_t n8, uint32_t ntris, const float4 *__restrict__ bvh8, uint32_t *__restrict__ err) {
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= n8) return;
-  float4 *o = bvh8 + 16ull * f;
+  const float4 *o = bvh8 + 16ull * f;
   for (int s = 0; s < 8; s++) {
-    float4 w = o[2 * s + 1];
-    const int32_t ref = __float_as_int(w.z);
+    const int32_t ref = __float_as_int(o[2 * s + 1].z);
     if (ref == INT_MIN) continue;
-    if (ref < 0) {
-      if ((uint32_t)~ref >= ntris) atomicOr(err, 2u);
-      continue;
-    }
-    if ((uint32_t)ref >= n8) {
-      atomicOr(err, 2u);
-      continue;
-    }
-    const float4 *c = bvh8 + 16ull * ref;
-    int filled = 8;
-    for (int q = 1; q < 8; q++) {
-      if (__float_as_int(c[2 * q + 1].z) == INT_MIN) {
-        filled = q;
-        break;
-      }
-    }
-    w.z = __int_as_float((ref << 3) | (filled - 1));
-    o[2 * s + 1] = w;
+    if (ref < 0 ? (uint32_t)~ref >= ntris : (uint32_t)ref >= n8) atomicOr(err, 2u);
   }
 }
 
@@ -228,16 +279,16 @@ __global__ void k_quantize8(const float4 *__restrict__ wide, uint32_t n8, uint4 
   const float4 *W = wide + 16ull * f;
   float box[8][6];
   int32_t ref[8];
-  int filled = 0;
+  uint32_t fmask = 0;
   for (int s = 0; s < 8; s++) {
     const float4 a = W[2 * s], b = W[2 * s + 1];
     box[s][0] = a.x, box[s][1] = a.y, box[s][2] = a.z;
     box[s][3] = a.w, box[s][4] = b.x, box[s][5] = b.y;
     ref[s] = __float_as_int(b.z);
-    if (ref[s] != INT_MIN) filled = s + 1;
+    if (ref[s] != INT_MIN) fmask |= 1u << s;
   }
   uint32_t w[24];
-  if (!quantize_node8(box, ref, filled, w)) atomicOr(err, 8u);
+  if (!quantize_node8(box, ref, fmask, w)) atomicOr(err, 8u);
   uint4 *o = out + 6ull * f;
   for (int i = 0; i < 6; i++) o[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
 }
@@ -253,7 +304,7 @@ cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint3
                             int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
   *n8_out = 0;
   *levels_out = 0;
-  *root_out = 7;  // node 0, all slots decoded
+  *root_out = 0;  // node 0
   if (d.ntris == 0 || cap == 0 || !bvh8) return cudaErrorInvalidValue;
   if (d.root_ref < 0) {
     // One triangle: a single node with the root leaf in slot 0.
@@ -275,7 +326,7 @@ cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint3
     if (e != cudaSuccess) return e;
     *n8_out = 1;
     *levels_out = 1;
-    *root_out = 0;  // node 0, one filled slot
+    *root_out = 0;  // node 0: one leaf in slot 0
     return cudaSuccess;
   }
   const uint32_t n_pairs = d.ntris - 1;
@@ -373,15 +424,29 @@ cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n
 
 }  // namespace rtgb
 
-// Host form of the node quantization, so that its containment guarantee can
-// be checked without a GPU (rt_scenes.h).
-extern "C" uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t filled, uint32_t *out) {
-  if (!boxes || !refs || !out || filled < 1 || filled > 8) return 0;
+// Host forms of the node quantization and the octant slot assignment, so
+// that the containment guarantee and the fold can be checked without a GPU
+// (rt_scenes.h).
+extern "C" uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t fmask, uint32_t *out) {
+  fmask &= 0xffu;
+  if (!boxes || !refs || !out || fmask == 0) return 0;
   float box[8][6] = {};
   int32_t ref[8];
   for (uint32_t s = 0; s < 8; s++) {
-    ref[s] = s < filled ? refs[s] : INT_MIN;
-    for (int j = 0; j < 6; j++) box[s][j] = s < filled ? boxes[6 * s + j] : 0.0f;
+    const bool f = (fmask >> s) & 1u;
+    ref[s] = f ? refs[s] : INT_MIN;
+    for (int j = 0; j < 6; j++) box[s][j] = f ? boxes[6 * s + j] : 0.0f;
   }
-  return rtgb::quantize_node8(box, ref, (int)filled, out) ? 1u : 0u;
+  return rtgb::quantize_node8(box, ref, fmask, out) ? 1u : 0u;
+}
+
+extern "C" uint32_t rtgbAssignOctantSlots(const float *boxes, uint32_t cnt, int32_t *slot_of) {
+  if (!boxes || !slot_of || cnt < 1 || cnt > 8) return 0;
+  float box[8][6] = {};
+  for (uint32_t i = 0; i < cnt; i++)
+    for (int j = 0; j < 6; j++) box[i][j] = boxes[6 * i + j];
+  int so[8];
+  rtgb::assign_octant_slots(box, (int)cnt, so);
+  for (uint32_t i = 0; i < cnt; i++) slot_of[i] = so[i];
+  return 1;
 }

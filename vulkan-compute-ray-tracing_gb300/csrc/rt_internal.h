@@ -32,11 +32,13 @@ enum : uint32_t {
 //           rounding.
 //   leaf_tri  original triangle index of leaf k.
 //   bvh8    the same tree with levels folded into nodes of up to eight
-//           children (bvh8.cu), 96 B per node: origin, per-axis exponents,
-//           8-bit child bounds rounded outward, child refs; filled slots
-//           first, breadth-first numbered, root node 0; inner refs are
-//           (node << 3) | (filled slots - 1), leaf refs the bvh2 ones (~k).
-//           Used by the per-lane 8-wide caster.
+//           children (bvh8.cu), 96 B per node: origin, per-axis exponents
+//           and the filled-slot mask, 8-bit child bounds rounded outward,
+//           child refs; slots assigned by octant so that a ray meets the
+//           children in about the order s ^ (its direction's sign bits);
+//           breadth-first numbered, root node 0; inner refs are node
+//           numbers, leaf refs the bvh2 ones (~k). Used by the per-lane
+//           8-wide caster.
 struct DevScene {
   const rt_triangle *tris;
   const rt_material *mats;
@@ -53,7 +55,7 @@ struct DevScene {
   uint32_t depth;
   const float4 *bvh8;
   uint32_t n8, levels8;  // bvh8 nodes and levels (0 when absent)
-  int32_t root8;         // encoded ref of the bvh8 root: (0 << 3) | (filled slots - 1)
+  int32_t root8;         // the bvh8 root node (0)
 };
 
 // ---------------------------------------------------------------- bvh8.cu
@@ -88,7 +90,17 @@ struct TraceOpts {
   int wide_refill = 4;     // idle lanes of a k_trace_wide warp that trigger a fetch of new rays (1..32)
   uint32_t wide_min_tris = 1u << 17;  // scenes from this many triangles up use the 8-wide caster
   uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
+  int block = 128;  // threads per block of the casting kernels (64, 128 or 256)
+  int stack = 0;    // traversal stack entries (16, 32 or 64; 0: the smallest that holds the tree)
 };
+
+// Stack entries a cast of this scene runs with: trace.stack raised to the
+// smallest of 16, 32, 64 that holds the tree (binary depth for the packet
+// and per-lane kernels; the 8-wide caster's group stack needs its levels).
+inline int trace_stack_entries(const TraceOpts &o, const DevScene &sc) {
+  const int need = sc.depth <= 16 ? 16 : (sc.depth <= 32 ? 32 : 64);
+  return o.stack > need ? (o.stack <= 32 ? 32 : 64) : need;
+}
 
 // `counter` is a device word private to this launch (work distribution);
 // `refine` recomputes t, u, v of the winning triangle in fp64.
