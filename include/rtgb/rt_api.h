@@ -178,7 +178,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   leaf when reached. Results are identical either way
  *   "trace.minblocks" 16, 12 (default) or 10: resident 128-thread blocks per
  *                   SM the per-lane caster is compiled for (register budget)
- *   "trace.packet_minblocks"  the same for the packet caster (default 10)
+ *   "trace.packet_minblocks"  the same for the packet caster (default 12)
  *   "trace.host_chunk"  rays per pipelined chunk of rtTraceClosestHost
  *                   (65536 .. 2^26, default 2^21)
  *   "trace.defer"   1 (default) = 32-ray chunks that fail the packet test are
@@ -195,6 +195,9 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   per SM the 8-wide caster is compiled for
  *   "trace.wide_refill"  idle lanes of an 8-wide caster warp that trigger
  *                   a fetch of new rays (1..32, default 4)
+ *   "trace.wide_visits"  node steps a lane of the 8-wide caster takes per
+ *                   loop iteration before the warp's shared leaf pool and
+ *                   refill bookkeeping run (1, or 2 default)
  *   "trace.wide_min_tris"  scenes with at least this many triangles use
  *                   the 8-wide caster (default 2^17; smaller trees stay in
  *                   cache, where the binary layout is faster); it applies
@@ -213,8 +216,16 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   1 wavefront (per-bounce kernels over compacted queues),
  *                   2 (default) wavefront from render.wavefront_pixels up;
  *                   images are identical in every mode
- *   "render.wavefront_pixels"  the mode-2 threshold (default 2^20 pixels);
- *                   also splits batches and the render server's steps
+ *   "render.wavefront_pixels"  the mode-2 threshold of rtRender (default
+ *                   2^20 pixels)
+ *   "render.batch_wavefront_pixels"  the split of batches and of the
+ *                   render server's steps: jobs from this many pixels up run
+ *                   as wavefronts side by side on side streams, the rest in
+ *                   one persistent tile launch (default 1: every job; jobs
+ *                   that run side by side fill the GPU at any size, where a
+ *                   render alone keeps render.wavefront_pixels)
+ *   "render.batch_streams"  side streams a batch (rtBatchCreate) spreads
+ *                   its wavefront jobs over, 1..16 (default 16)
  *   "bvh.builder"   tree built by rtUploadScene when no nodes are given:
  *                   0 (default) the reference's Bvh.h tree, node-for-node;
  *                   1 a linear BVH over Morton-ordered centroids,
@@ -235,7 +246,7 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value);
 /* Autotuner (no counterpart in the reference, whose launch shape is fixed at
  * compile time, ray-trace-compute.comp:3, 262). Times the closest-hit
  * launch shapes on the caller's own device rays (coordinate descent over
- * trace.block, trace.stack, trace.wide, trace.wide_minblocks, trace.defer,
+ * trace.block, trace.stack, trace.wide, trace.wide_minblocks, trace.wide_visits, trace.defer,
  * trace.spec, trace.minblocks, trace.packet_minblocks, trace.sort; `reps` timed casts
  * per candidate after one warm-up) and keeps the fastest. Hits are identical
  * in every shape; d_hits receives them. The rates before and after tuning
@@ -297,9 +308,9 @@ typedef struct rt_render_job {
 } rt_render_job;
 
 /* Renders every job; per job the image equals rtRender of that job alone.
- * Jobs that rtRender would give the wavefront kernels ("render.mode" 1, or 2
- * and at least 2^20 pixels) run one after another on a side stream, while
- * one persistent launch covers the pixel tiles of all other jobs; the two
+ * Jobs from render.batch_wavefront_pixels up (default: all) run as
+ * wavefronts spread over render.batch_streams side streams (default 16),
+ * while one persistent launch covers the pixel tiles of the others; the two
  * overlap on the GPU. The reference renders one scene per dispatch
  * (src/main.cpp:228); this is the batched form. Returns when the jobs are
  * done. */

@@ -18,6 +18,21 @@ SPECS = [(31, 200, 0), (32, 3000, 4), (33, 20000, 16), (34, 1000, 2), (35, 60000
 SIZES = [(64, 48), (128, 128), (96, 80), (40, 200), (160, 96)]
 
 
+@pytest.fixture(params=[(1, 16), (1 << 20, 4)], ids=["all-wavefront", "tiles+sides"])
+def batch_split(request, ctx):
+    """Both ways a batch can share its jobs out (render.batch_wavefront_pixels,
+    render.batch_streams): every job a wavefront on 16 side streams (the
+    default), and jobs below 2^20 pixels in the persistent tile launch with
+    the rest on 4 side streams."""
+    keys = ("render.batch_wavefront_pixels", "render.batch_streams")
+    old = [ctx.get_tuning(k) for k in keys]
+    for k, v in zip(keys, request.param):
+        ctx.set_tuning(k, v)
+    yield request.param
+    for k, v in zip(keys, old):
+        ctx.set_tuning(k, v)
+
+
 def render_alone(ctx, sc, cam, W, H, spp, bounces, flags=0, sample_index=0):
     import torch
     acc = torch.zeros((H, W, 4), device="cuda")
@@ -27,7 +42,7 @@ def render_alone(ctx, sc, cam, W, H, spp, bounces, flags=0, sample_index=0):
     return acc.cpu().numpy()
 
 
-def test_batch_equals_individual_renders(rt, ctx):
+def test_batch_equals_individual_renders(rt, ctx, batch_split):
     import torch
     scs = scenes(rt, ctx, SPECS)
     try:
@@ -51,7 +66,7 @@ def test_batch_equals_individual_renders(rt, ctx):
             sc.release()
 
 
-def test_batch_graph_progressive_frames(rt, ctx):
+def test_batch_graph_progressive_frames(rt, ctx, batch_split):
     """Three graph replays (launch + device-side sample advance) equal one
     render of three times the samples."""
     import torch
@@ -80,15 +95,17 @@ def test_batch_graph_progressive_frames(rt, ctx):
 
 @pytest.mark.parametrize("mode", [1, 2])
 def test_hybrid_batch_with_wavefront_jobs(rt, ctx, mode):
-    """Jobs that rtRender would render with the wavefront kernels (all of
-    them in render.mode 1; the 1024x1024 one in mode 2) run on a side stream
-    next to the persistent launch; every image equals the job alone, for a
-    direct launch and for three progressive graph replays."""
+    """With the batch split at 2^20 pixels, the wavefront jobs (all of them
+    in render.mode 1; the 1024x1024 one in mode 2) run on side streams next
+    to the persistent launch over the others; every image equals the job
+    alone, for a direct launch and for three progressive graph replays."""
     import torch
     scs = scenes(rt, ctx, SPECS[:3])
     sizes = [(1024, 1024), (128, 96), (200, 40)]
     old = ctx.get_tuning("render.mode")
+    old_split = ctx.get_tuning("render.batch_wavefront_pixels")
     ctx.set_tuning("render.mode", mode)
+    ctx.set_tuning("render.batch_wavefront_pixels", 1 << 20)
     try:
         jobs, accs, want, want3 = [], [], [], []
         for i, (sc, (W, H)) in enumerate(zip(scs, sizes)):
@@ -115,6 +132,7 @@ def test_hybrid_batch_with_wavefront_jobs(rt, ctx, mode):
             assert np.array_equal(a.cpu().numpy().view(np.uint32), w.view(np.uint32))
     finally:
         ctx.set_tuning("render.mode", old)
+        ctx.set_tuning("render.batch_wavefront_pixels", old_split)
         for sc in scs:
             sc.release()
 

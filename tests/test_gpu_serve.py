@@ -39,17 +39,23 @@ REQS = [(0, 64, 48, 5, 8), (1, 96, 64, 3, 6), (2, 80, 80, 7, 8), (0, 32, 128, 2,
         (1, 48, 48, 9, 3), (2, 100, 60, 1, 8)]
 
 
-@pytest.mark.parametrize("max_active,spp_step,mode", [(0, 2, 2), (3, 1, 2), (1, 0, 2), (0, 2, 1), (5, 3, 1)])
-def test_results_equal_alone_in_the_mix(rt, ctx, serve_mod, max_active, spp_step, mode):
-    """render.mode 1 sends every request through the wavefront side streams
-    (several at once), mode 2 at these sizes through the persistent launch."""
+@pytest.mark.parametrize("max_active,spp_step,mode,split", [(0, 2, 2, 1 << 20), (3, 1, 2, 1 << 20), (1, 0, 2, 1),
+                                                            (0, 2, 1, 1), (5, 3, 1, 1), (5, 3, 2, 1)])
+def test_results_equal_alone_in_the_mix(rt, ctx, serve_mod, max_active, spp_step, mode, split):
+    """The default split (render.batch_wavefront_pixels 1) and render.mode 1
+    send every request through the wavefront side streams (several at
+    once); a split at 2^20 pixels sends these sizes through the persistent
+    launch."""
     datas = [scene_data(rt, 40 + i, n, k) for i, (n, k) in enumerate([(500, 2), (3000, 0), (8000, 5), (1500, 1)])]
     old_mode = ctx.get_tuning("render.mode")
+    old_split = ctx.get_tuning("render.batch_wavefront_pixels")
     ctx.set_tuning("render.mode", mode)
+    ctx.set_tuning("render.batch_wavefront_pixels", split)
     try:
         run_mix(rt, ctx, serve_mod, datas, max_active, spp_step)
     finally:
         ctx.set_tuning("render.mode", old_mode)
+        ctx.set_tuning("render.batch_wavefront_pixels", old_split)
 
 
 def run_mix(rt, ctx, serve_mod, datas, max_active, spp_step):

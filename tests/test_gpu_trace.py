@@ -352,8 +352,8 @@ def test_alt_tree_mode_same_hits(rt, orc, ctx, builder):
 def test_autotune_trace_keeps_hits(rt, orc, ctx):
     """The autotuner's candidates are timing choices only: after tuning, the
     hits equal the ones cast with the settings it started from."""
-    keys = ("trace.block", "trace.stack", "trace.wide", "trace.wide_minblocks", "trace.defer", "trace.spec",
-            "trace.minblocks", "trace.packet_minblocks", "trace.sort")
+    keys = ("trace.block", "trace.stack", "trace.wide", "trace.wide_minblocks", "trace.wide_visits", "trace.defer",
+            "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort")
     old = [ctx.get_tuning(k) for k in keys]
     tris, sc = mesh_scene(rt, ctx, 6, 3)
     try:
@@ -365,7 +365,7 @@ def test_autotune_trace_keeps_hits(rt, orc, ctx):
         d_hits = torch.zeros((len(rays), 4), dtype=torch.float32, device="cuda")
         before, after = rt.autotune_trace(sc, d_rays, len(rays), d_hits, reps=1)
         assert before > 0 and after > 0
-        allowed = {"trace.wide_minblocks": (8, 6, 5), "trace.minblocks": (16, 12, 10),
+        allowed = {"trace.wide_minblocks": (8, 6, 5), "trace.minblocks": (16, 12, 10), "trace.wide_visits": (1, 2),
                    "trace.packet_minblocks": (16, 12, 10), "trace.block": (64, 128, 256),
                    "trace.stack": (0, 32, 64)}
         for k in keys:
@@ -380,13 +380,13 @@ def test_autotune_trace_keeps_hits(rt, orc, ctx):
 
 @pytest.mark.parametrize("level,wide_min", [(6, 0), (6, 1 << 30), (4, 1 << 30)], ids=["bvh8", "binary", "shallow"])
 def test_block_size_and_stack_depth_keep_hits(rt, ctx, level, wide_min):
-    """The autotuner's block-size (64/128/256 threads) and stack-depth
-    (16/32/64 entries, raised to what the tree needs) axes: every candidate
-    returns the same hits bit for bit, on the 8-wide caster and on the
-    binary packet and per-lane kernels, including a tree shallow enough for
-    the 16-entry stack."""
+    """The autotuner's block-size (64/128/256 threads), stack-depth
+    (16/32/64 entries, raised to what the tree needs) and 8-wide visits
+    axes: every candidate returns the same hits bit for bit, on the 8-wide
+    caster and on the binary packet and per-lane kernels, including a tree
+    shallow enough for the 16-entry stack."""
     tris, sc = mesh_scene(rt, ctx, level, 4)
-    keys = ("trace.block", "trace.stack", "trace.wide_min_tris")
+    keys = ("trace.block", "trace.stack", "trace.wide_min_tris", "trace.wide_visits")
     old = [ctx.get_tuning(k) for k in keys]
     try:
         ctx.set_tuning("trace.wide_min_tris", wide_min)
@@ -395,12 +395,16 @@ def test_block_size_and_stack_depth_keep_hits(rt, ctx, level, wide_min):
         cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 128, 96)
         rays = np.concatenate([rt.gen_camera_rays(cam, 128, 96), rt.gen_random_rays(12, 20000)])
         base = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+        refined = gpu_trace(ctx, sc, rays)
         for block in (64, 128, 256):
             for stack in (0, 16, 32, 64):
                 ctx.set_tuning("trace.block", block)
                 ctx.set_tuning("trace.stack", stack)
+                ctx.set_tuning("trace.wide_visits", 2 if stack % 32 else 1)
                 got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
                 assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (block, stack)
+                # The default (fp64 re-evaluated) results agree as well.
+                assert np.array_equal(gpu_trace(ctx, sc, rays).view(np.uint32), refined.view(np.uint32))
     finally:
         for k, v in zip(keys, old):
             ctx.set_tuning(k, v)

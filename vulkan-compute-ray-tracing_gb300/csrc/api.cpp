@@ -781,6 +781,21 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.wide_refill = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.wide_visits") {
+    if (value != 1 && value != 2) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.wide_visits = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "render.batch_streams") {
+    if (value < 1 || value > 16) return RT_ERR_INVALID_ARGUMENT;
+    ctx->render_opts.batch_streams = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "render.batch_wavefront_pixels") {
+    if (value < 1 || value > (1ll << 31)) return RT_ERR_INVALID_ARGUMENT;
+    ctx->render_opts.batch_wavefront_pixels = (uint64_t)value;
+    return RT_SUCCESS;
+  }
   if (k == "trace.block") {
     if (value != 64 && value != 128 && value != 256) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.block = (int)value;
@@ -875,6 +890,18 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
     *value = ctx->trace_opts.block;
     return RT_SUCCESS;
   }
+  if (k == "trace.wide_visits") {
+    *value = ctx->trace_opts.wide_visits;
+    return RT_SUCCESS;
+  }
+  if (k == "render.batch_streams") {
+    *value = ctx->render_opts.batch_streams;
+    return RT_SUCCESS;
+  }
+  if (k == "render.batch_wavefront_pixels") {
+    *value = (int64_t)ctx->render_opts.batch_wavefront_pixels;
+    return RT_SUCCESS;
+  }
   if (k == "trace.stack") {
     *value = ctx->trace_opts.stack;
     return RT_SUCCESS;
@@ -952,7 +979,7 @@ bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort, bo
   if (sort) *sort = ctx->trace_opts.sort != 0;
   if (wide) *wide = ctx->trace_opts.wide != 0;
   if (min_tris) *min_tris = ctx->trace_opts.wide_min_tris;
-  return use_wavefront(ctx->render_opts, p);
+  return use_wavefront_batched(ctx->render_opts, p);
 }
 uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) {
   return nt ? slab_layout(nt, nm, nl, ns).total : 0;
@@ -972,9 +999,11 @@ struct rt_batch {
   uint32_t n = 0, total_tiles = 0, max_depth = 0;
   std::vector<BatchJob> wf;    // wavefront jobs (host copies)
   BatchJob *d_wf = nullptr;    // their device copies: sample_index advances there
-  // Wavefront jobs alternate between kSides side streams, each with its own
-  // scratch and work counter (counter[64 * (1 + k)]).
-  static constexpr int kSides = 4;
+  // Wavefront jobs alternate between `sides` side streams (render.batch_streams,
+  // at most kSides), each with its own scratch and work counter
+  // (counter[64 * (1 + k)]).
+  static constexpr int kSides = 16;
+  int sides = 0;
   void *wf_scratch[kSides] = {};
   bool wf_sort = true;
   bool wf_wide = true;
@@ -1026,18 +1055,18 @@ rt_status make_jobs(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n, std::vec
   return RT_SUCCESS;
 }
 
-bool wavefront_job(const RenderOpts &o, const rt_render_params &p) { return use_wavefront(o, p); }
+bool wavefront_job(const RenderOpts &o, const rt_render_params &p) { return use_wavefront_batched(o, p); }
 
 cudaError_t batch_enqueue(rt_ctx *ctx, rt_batch *b, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
-  const int sides = (int)std::min<size_t>(b->wf.size(), rt_batch::kSides);
+  const int sides = b->sides;
   if (sides) {
     if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return e;
     for (int k = 0; k < sides; k++)
       if ((e = cudaStreamWaitEvent(b->side[k], b->fork, 0)) != cudaSuccess) return e;
     for (size_t j = 0; j < b->wf.size() && e == cudaSuccess; j++) {
       const BatchJob &J = b->wf[j];
-      const int k = (int)(j % rt_batch::kSides);
+      const int k = (int)(j % (size_t)sides);
       e = launch_render_wavefront(J.sc, J.cam, J.p, J.accum, ctx->d_segments, b->counter + 64 * (1 + k), ctx->d_err,
                                   b->wf_scratch[k], b->wf_sort, b->wf_wide && J.sc.ntris >= b->wf_wide_min,
                                   b->side[k], &b->d_wf[j].p.sample_index);
@@ -1110,7 +1139,9 @@ rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs,
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_wf, b->wf.data(), sizeof(BatchJob) * b->wf.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    const int sides = (int)std::min<size_t>(b->wf.size(), rt_batch::kSides);
+    const int sides =
+        (int)std::min<size_t>(b->wf.size(), (size_t)std::clamp(ropts.batch_streams, 1, rt_batch::kSides));
+    b->sides = sides;
     for (int k = 0; k < sides && e == cudaSuccess; k++) {
       e = cudaMalloc(&b->wf_scratch[k], wavefront_scratch_bytes(max_wf));
       if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking);

@@ -5,7 +5,7 @@
 //   closest hit  coordinate descent over trace.block (threads per block,
 //                64/128/256), trace.stack (traversal stack entries 16/32/64,
 //                each raised to the smallest size that holds the tree),
-//                trace.wide, trace.wide_minblocks, trace.defer, trace.spec,
+//                trace.wide, trace.wide_minblocks, trace.wide_visits, trace.defer, trace.spec,
 //                trace.minblocks, trace.packet_minblocks and trace.sort,
 //                each candidate timed with CUDA events over `reps` casts
 //                after one warm-up cast;
@@ -94,6 +94,7 @@ rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, 
                         {"trace.stack", {0, 32, 64}},
                         {"trace.wide", {1, 0}},
                         {"trace.wide_minblocks", {8, 6, 5}},
+                        {"trace.wide_visits", {2, 1}},
                         {"trace.defer", {1, 0}},
                         {"trace.spec", {1, 0}},
                         {"trace.minblocks", {16, 12, 10}},

@@ -83,11 +83,12 @@ struct TraceOpts {
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
   int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
-  int packet_minblocks = 10;  // the same for the packet caster
+  int packet_minblocks = 12;  // the same for the packet caster
   int defer = 1;    // 1: chunks that fail the packet test go to the per-lane kernel; 0: traced in place
   int wide = 1;     // 1: per-lane chunks are cast over bvh8 with a warp leaf pool (k_trace_wide)
   int wide_minblocks = 6;  // resident 128-thread blocks per SM k_trace_wide is compiled for (8, 6 or 5)
   int wide_refill = 4;     // idle lanes of a k_trace_wide warp that trigger a fetch of new rays (1..32)
+  int wide_visits = 2;     // node steps per lane per k_trace_wide loop iteration (1 or 2)
   uint32_t wide_min_tris = 1u << 17;  // scenes from this many triangles up use the 8-wide caster
   uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
   int block = 128;  // threads per block of the casting kernels (64, 128 or 256)
@@ -153,12 +154,25 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
 struct RenderOpts {
   int mode = 2;                         // 0 megakernel, 1 wavefront, 2 choose by image size
   uint64_t wavefront_pixels = 1u << 20;  // mode 2: wavefront from this many pixels up
+  int batch_streams = 16;                // side streams a batch spreads its wavefront jobs over (1..16)
+  // Batches and the render server: jobs from this many pixels up run as
+  // wavefronts on side streams (the rest in the persistent tile launch).
+  // Jobs that run side by side keep the GPU busy at any size, and sorted
+  // bounce rays beat the megakernel's diverged lanes, so all of them do by
+  // default; a render alone keeps wavefront_pixels.
+  uint64_t batch_wavefront_pixels = 1;
 };
 // True when a render of these params goes to the wavefront kernels.
 inline bool use_wavefront(const RenderOpts &o, const rt_render_params &p) {
   if (p.flags & RT_COMPAT_STACK16) return false;  // the literal 16-entry traversal is megakernel-only
   const uint64_t pixels = (uint64_t)p.width * p.height;
   return pixels < (1ull << 31) && (o.mode == 1 || (o.mode == 2 && pixels >= o.wavefront_pixels));
+}
+// True when a job of a batch or a server step goes to the wavefront kernels.
+inline bool use_wavefront_batched(const RenderOpts &o, const rt_render_params &p) {
+  RenderOpts b = o;
+  b.wavefront_pixels = o.batch_wavefront_pixels;
+  return use_wavefront(b, p);
 }
 
 // Tree used when a scene is uploaded without nodes (rtSetTuning "bvh.builder").
@@ -208,9 +222,10 @@ uint32_t *ctx_err(rt_ctx *ctx);
 uint64_t ctx_budget(rt_ctx *ctx);
 int ctx_device(rt_ctx *ctx);
 cudaStream_t ctx_stream(rt_ctx *ctx);
-// True when rtRender would give a render of these params to the wavefront
-// kernels (render.mode 1, or 2 and >= 2^20 pixels; never the 16-entry
-// compat traversal); *sort receives trace.sort.
+// True when a batch or a server step gives a job of these params to the
+// wavefront kernels (render.mode 1, or 2 and at least
+// render.batch_wavefront_pixels; never the 16-entry compat traversal);
+// *sort receives trace.sort.
 bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort, bool *wide = nullptr,
                           uint32_t *min_tris = nullptr);
 // Device bytes rtUploadScene allocates for a scene of these counts.

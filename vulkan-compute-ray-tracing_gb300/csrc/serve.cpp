@@ -80,7 +80,7 @@ struct rt_server {
   uint32_t *d_counter = nullptr;  // [0] tile counter, [64 * (1 + k)] side k's work counter
   int device = 0;
   // Wavefront side streams, their scratch (grown on demand) and join events.
-  static constexpr int kSides = 4;
+  static constexpr int kSides = 16;
   cudaStream_t side[kSides] = {};
   cudaEvent_t fork = nullptr, join[kSides] = {};
   void *scratch[kSides] = {};

@@ -32,7 +32,7 @@ constexpr int kTraceBlock = 128;
 // (64, 128 or 256 threads, "trace.block") with per-warp shared memory
 // sized dynamically, so the budget is set per thread with __maxnreg__.
 template <int MINB>
-constexpr int regs_for() {
+__host__ __device__ constexpr int regs_for() {
   return (65536 / (128 * MINB)) / 8 * 8;
 }
 
@@ -65,20 +65,6 @@ __device__ __forceinline__ void refine_fp64(const rt_triangle *__restrict__ tris
   t = __double2float_rn(__dmul_rn(ddot(n, p), idet));
 }
 
-// Every hit of a cast: t, u, v of its triangle recomputed in fp64 from the
-// ray (the hit's fp32 values are replaced; misses are left alone).
-__global__ void k_refine_hits(const rt_triangle *__restrict__ tris, uint32_t ntris, const float4 *__restrict__ rays,
-                              uint32_t n, int4 *__restrict__ hits) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int4 h = hits[i];
-  if (h.x < 0 || (uint32_t)h.x >= ntris) return;
-  const float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
-  float t, u, v;
-  refine_fp64(tris, h.x, mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), t, u, v);
-  hits[i] = make_int4(h.x, __float_as_int(t), __float_as_int(u), __float_as_int(v));
-}
-
 constexpr int kDone = INT_MIN;  // no node left: the ray is finished
 
 // Persistent warps with per-lane refill: each lane owns one ray at a time;
@@ -90,7 +76,8 @@ constexpr int kDone = INT_MIN;  // no node left: the ray is finished
 template <int STACK>
 __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4 *__restrict__ rays, uint32_t n,
                                                        int4 *__restrict__ hits, uint32_t *__restrict__ counter,
-                                                       uint32_t *err, int refill, const uint32_t *__restrict__ perm) {
+                                                       uint32_t *err, int refill, const uint32_t *__restrict__ perm,
+                                                       bool refine) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const float4 *__restrict__ bvh = sc.bvh2;
@@ -166,7 +153,10 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
       if (node == kDone) {
         int4 h;
         if (best >= 0) {
-          h = make_int4(__ldg(sc.leaf_tri + best), __float_as_int(closest), __float_as_int(bu), __float_as_int(bv));
+          const int tri = __ldg(sc.leaf_tri + best);
+          float t = closest, u = bu, v = bv;
+          if (refine) refine_fp64(sc.tris, tri, r.o, r.d, t, u, v);
+          h = make_int4(tri, __float_as_int(t), __float_as_int(u), __float_as_int(v));
         } else {
           h = make_int4(-1, 0, 0, 0);
         }
@@ -192,10 +182,15 @@ __device__ __forceinline__ void load_ray(const float4 *__restrict__ rays, uint32
   tmax = r1.w;
 }
 
-__device__ __forceinline__ void store_hit(const DevScene &sc, int4 *__restrict__ hits, uint32_t i, int k,
-                                          float closest, float u, float v) {
-  hits[i] = k >= 0 ? make_int4(__ldg(sc.leaf_tri + k), __float_as_int(closest), __float_as_int(u), __float_as_int(v))
-                   : make_int4(-1, 0, 0, 0);
+__device__ __forceinline__ void store_hit(const DevScene &sc, int4 *__restrict__ hits, uint32_t i, int k, f3 o, f3 d,
+                                          float closest, float u, float v, bool refine) {
+  int4 h = make_int4(-1, 0, 0, 0);
+  if (k >= 0) {
+    const int tri = __ldg(sc.leaf_tri + k);
+    if (refine) refine_fp64(sc.tris, tri, o, d, closest, u, v);
+    h = make_int4(tri, __float_as_int(closest), __float_as_int(u), __float_as_int(v));
+  }
+  hits[i] = h;
 }
 
 // First kernel of a whole-warp cast: each warp takes 32 consecutive rays (in
@@ -210,7 +205,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_packets(DevScene sc, const
                                                                    uint32_t *__restrict__ counter, uint32_t *err,
                                                                    const uint32_t *__restrict__ perm,
                                                                    uint32_t *__restrict__ list,
-                                                                   uint32_t *__restrict__ list_count) {
+                                                                   uint32_t *__restrict__ list_count, bool refine) {
   extern __shared__ int s_dyn_stack[];  // STACK entries per warp
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int *const s_stack = s_dyn_stack + warp * STACK;
@@ -241,7 +236,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_packets(DevScene sc, const
     } else {
       k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
     }
-    if (active) store_hit(sc, hits, i, k, closest, u, v);
+    if (active) store_hit(sc, hits, i, k, o, d, closest, u, v, refine);
   }
 }
 
@@ -254,7 +249,8 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_lanes(DevScene sc, const f
                                                                    uint32_t *__restrict__ counter, uint32_t *err,
                                                                    const uint32_t *__restrict__ perm,
                                                                    const uint32_t *__restrict__ list,
-                                                                   const uint32_t *__restrict__ list_count, int spec) {
+                                                                   const uint32_t *__restrict__ list_count, int spec,
+                                                                   bool refine) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t chunks = list ? min(*list_count, (n + 31) / 32) : (n + 31) / 32;
   for (;;) {
@@ -282,7 +278,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_lanes(DevScene sc, const f
     } else {
       k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
     }
-    if (active) store_hit(sc, hits, i, k, closest, u, v);
+    if (active) store_hit(sc, hits, i, k, o, d, closest, u, v, refine);
   }
 }
 
@@ -332,8 +328,18 @@ __device__ __forceinline__ float qbyte(uint32_t w, int b) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)b)) - 8388608.0f;
 }
 
-constexpr int kPool = 512;       // leaf pool entries per warp (power of two)
-constexpr int kWideWarpSmem = 64 * 16 + 32 * 8 + 32 * 16 + kPool * 4;  // 3,840 bytes
+// Leaf pool entries per warp (power of two): at most 31 are left after the
+// leaf rounds of an iteration, and each of its VISITS node steps adds at
+// most 8 per lane.
+template <int VISITS>
+__host__ __device__ constexpr int pool_entries() {
+  return VISITS == 1 ? 512 : 1024;
+}
+constexpr int kFinish = 64;  // finished-ray ring per warp (power of two, >= 64)
+template <int VISITS>
+__host__ __device__ constexpr int wide_warp_smem() {
+  return 64 * 16 + 32 * 8 + 32 * 16 + pool_entries<VISITS>() * 4 + kFinish * 4;
+}
 
 // ref[s] without local memory: a select tree on the bits of s.
 __device__ __forceinline__ int32_t pick8(const int32_t (&ref)[8], uint32_t s) {
@@ -376,7 +382,7 @@ __device__ __forceinline__ int32_t pick8(const int32_t (&ref)[8], uint32_t s) {
 // LEAF_OUT: hits are int2 (leaf k, fp32 t) for the wavefront's shading (k =
 // -1 and the ray's tmax when nothing is hit), and the batch size is the
 // device word *d_n (capped at n); otherwise int4 rt_hit records.
-template <int GSTACK, int MINB, bool LEAF_OUT>
+template <int GSTACK, int MINB, bool LEAF_OUT, int VISITS>
 __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const float4 *__restrict__ rays,
                                                                uint32_t n, const uint32_t *d_n,
                                                                void *__restrict__ hits_out,
@@ -384,21 +390,39 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
                                                                const uint32_t *__restrict__ perm,
                                                                const uint32_t *__restrict__ list,
                                                                const uint32_t *__restrict__ list_count,
-                                                               int refill) {
-  // Per warp (kWideWarpSmem bytes, dynamic): the lanes' rays (32 x 2
-  // float4), closest-hit keys (32 x u64), winning t/u/v/leaf (32 x float4)
-  // and the leaf pool (kPool x u32).
+                                                               int refill, bool refine) {
+  // Per warp (wide_warp_smem bytes, dynamic): the lanes' rays (32 x 2
+  // float4), closest-hit keys (32 x u64), winning t/u/v/leaf (32 x float4),
+  // the leaf pool (kPool x u32) and the ring of finished rays waiting for
+  // their fp64 re-evaluation (kFinish x u32).
   extern __shared__ float4 s_wide[];
   uint32_t lane;
   asm("mov.u32 %0, %%laneid;" : "=r"(lane));
   const uint32_t warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  float4 *const wbase = s_wide + warp * (kWideWarpSmem / 16);
+  constexpr int kPool = pool_entries<VISITS>();
+  float4 *const wbase = s_wide + warp * (wide_warp_smem<VISITS>() / 16);
   float4(*ray_s)[2] = reinterpret_cast<float4(*)[2]>(wbase);
   volatile unsigned long long *key_v = reinterpret_cast<unsigned long long *>(wbase + 64);
   unsigned long long *key_a = reinterpret_cast<unsigned long long *>(wbase + 64);
   float4 *hit_s = wbase + 80;
   uint32_t *pool = reinterpret_cast<uint32_t *>(wbase + 112);
+  uint32_t *finish = pool + kPool;
+  uint32_t fhead = 0, ftail = 0;
+  // fp64 re-evaluation of 32 queued finished rays (or the `cnt` left at the
+  // end), one per lane: converged, so the few fp64 operations of each ray
+  // overlap the other warps' work instead of occupying the pipe for one lane.
+  auto refine_round = [&](uint32_t cnt) {
+    if (lane < cnt) {
+      const uint32_t i = finish[(fhead + lane) & (kFinish - 1)];
+      int4 h = static_cast<int4 *>(hits_out)[i];
+      const float4 r0 = __ldg(rays + 2ull * i), r1 = __ldg(rays + 2ull * i + 1);
+      float t, u, v;
+      refine_fp64(sc.tris, h.x, mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), t, u, v);
+      static_cast<int4 *>(hits_out)[i] = make_int4(h.x, __float_as_int(t), __float_as_int(u), __float_as_int(v));
+    }
+    fhead += cnt;
+  };
   const float INF = __int_as_float(0x7f800000);
   if (d_n) n = min(n, *d_n);
   const uint32_t total = list ? min(*list_count, (n + 31) / 32) * 32u : n;
@@ -409,12 +433,13 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
 
   uint32_t gstack[GSTACK];
   TraceRay r = make_ray(mk3(0.0f, 0.0f, 0.0f), mk3(1.0f, 0.0f, 0.0f), 0.0f);
-  int node = -1, gsp = 0, ray_i = -1;
+  int node = -1, gsp = 0, ray_i = -1, finish_i = 0;
   uint32_t gnode = 0, gmask = 0, oct = 0;
   uint32_t steps = 0, mlp1 = 0, head = 0, tail = 0;
   bool exhausted = false;
   for (;;) {
     // A ray with no node, no group left and its last pooled leaf tested.
+    bool queued = false;
     if (ray_i >= 0 && node < 0 && gmask == 0 && gsp == 0 && (int)(head - mlp1) >= 0) {
       const unsigned long long key = key_v[lane];
       const float tmax = ray_s[lane][1].w;
@@ -427,8 +452,21 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
         int4 h = make_int4(-1, 0, 0, 0);
         if (got) h = make_int4((int)(uint32_t)key, __float_as_int(w.x), __float_as_int(w.y), __float_as_int(w.z));
         static_cast<int4 *>(hits_out)[ray_i] = h;
+        queued = got && refine;
       }
+      if (queued) finish_i = ray_i;
       ray_i = -1;
+    }
+    if (!LEAF_OUT && refine) {
+      const uint32_t qm = __ballot_sync(0xffffffffu, queued);
+      if (qm) {
+        if (queued) finish[(ftail + __popc(qm & lt_mask)) & (kFinish - 1)] = (uint32_t)finish_i;
+        ftail += __popc(qm);
+        if (ftail - fhead >= 32u) {
+          __syncwarp();
+          refine_round(32u);
+        }
+      }
     }
     // Idle lanes claim new rays.
     const uint32_t idle = __ballot_sync(0xffffffffu, ray_i < 0);
@@ -462,128 +500,138 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
         }
       }
     }
-    if (exhausted && __all_sync(0xffffffffu, ray_i < 0)) return;
+    if (exhausted && __all_sync(0xffffffffu, ray_i < 0)) {
+      if (!LEAF_OUT && refine && ftail != fhead) {
+        __syncwarp();
+        refine_round(ftail - fhead);
+      }
+      return;
+    }
     __syncwarp();
 
-    // One node per lane that holds one.
-    uint32_t leafmask = 0;
-    int32_t ref[8];
-    if (ray_i >= 0 && node >= 0) {
-      if ((uint32_t)node >= n8 || ++steps > step_cap) {
-        atomicOr(err, (uint32_t)node >= n8 ? KERR_BAD_INDEX : KERR_TIMEOUT);
-        node = -1;
-        gmask = 0;
-        gsp = 0;
-      } else {
-        const float closest = ord_inv((uint32_t)(key_v[lane] >> 32));
-        const int node_idx = node;
-        const float4 *N = bvh8 + 6ll * node;
-        // The 96-byte quantized node in three 256-bit loads: a child's plane
-        // o + q * 2^e is entered at (o - ray.o) / d + q * (2^e / d), one FMA
-        // per plane on the byte q.
-        float4 q0, q1, q2, q3, q4, q5;
-        load_slot8(N, q0, q1);
-        load_slot8(N + 2, q2, q3);
-        load_slot8(N + 4, q4, q5);
-        const uint32_t ew = __float_as_uint(q0.w);
-        const uint32_t fmask = ew >> 24;
-        const float sx = r.ix * pow2i((int)(int8_t)(ew & 0xffu));
-        const float sy = r.iy * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
-        const float sz = r.iz * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
-        const float ax = (q0.x - r.o.x) * r.ix, ay = (q0.y - r.o.y) * r.iy, az = (q0.z - r.o.z) * r.iz;
-        // Near and far byte words per axis (slots 0-3, 4-7): lo for a
-        // positive 1/d, hi for a negative one.
-        const bool fx = (oct & 1u) != 0, fy = (oct & 2u) != 0, fz = (oct & 4u) != 0;
-        const uint32_t lx0 = __float_as_uint(q1.x), lx1 = __float_as_uint(q1.y);
-        const uint32_t ly0 = __float_as_uint(q1.z), ly1 = __float_as_uint(q1.w);
-        const uint32_t lz0 = __float_as_uint(q2.x), lz1 = __float_as_uint(q2.y);
-        const uint32_t hx0 = __float_as_uint(q2.z), hx1 = __float_as_uint(q2.w);
-        const uint32_t hy0 = __float_as_uint(q3.x), hy1 = __float_as_uint(q3.y);
-        const uint32_t hz0 = __float_as_uint(q3.z), hz1 = __float_as_uint(q3.w);
-        const uint32_t nw[6] = {fx ? hx0 : lx0, fx ? hx1 : lx1, fy ? hy0 : ly0,
-                                fy ? hy1 : ly1, fz ? hz0 : lz0, fz ? hz1 : lz1};
-        const uint32_t fw[6] = {fx ? lx0 : hx0, fx ? lx1 : hx1, fy ? ly0 : hy0,
-                                fy ? ly1 : hy1, fz ? lz0 : hz0, fz ? lz1 : hz1};
-        ref[0] = __float_as_int(q4.x), ref[1] = __float_as_int(q4.y), ref[2] = __float_as_int(q4.z);
-        ref[3] = __float_as_int(q4.w), ref[4] = __float_as_int(q5.x), ref[5] = __float_as_int(q5.y);
-        ref[6] = __float_as_int(q5.z), ref[7] = __float_as_int(q5.w);
-        uint32_t ibits = 0, nearest = 0;
-        float tbest = INF;
-#pragma unroll
-        for (int s = 0; s < 8; s++) {
-          const int w = s >> 2, b = s & 3;
-          const float tnx = fmaf(qbyte(nw[0 + w], b), sx, ax), tfx = fmaf(qbyte(fw[0 + w], b), sx, ax);
-          const float tny = fmaf(qbyte(nw[2 + w], b), sy, ay), tfy = fmaf(qbyte(fw[2 + w], b), sy, ay);
-          const float tnz = fmaf(qbyte(nw[4 + w], b), sz, az), tfz = fmaf(qbyte(fw[4 + w], b), sz, az);
-          const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
-          const float tf = min3f(tfx, tfy, fminf(tfz, closest));
-          if (tn <= tf && ((fmask >> s) & 1u)) {
-            if (ref[s] >= 0) {
-              ibits |= 1u << ((uint32_t)s ^ oct);
-              if (tn < tbest) {
-                tbest = tn;
-                nearest = (uint32_t)s;
+#pragma unroll 1
+    for (int visit = 0; visit < VISITS; visit++) {
+      if (visit > 0 && !__any_sync(0xffffffffu, ray_i >= 0 && node >= 0)) break;
+      // One node per lane that holds one.
+      uint32_t leafmask = 0;
+      int32_t ref[8];
+      if (ray_i >= 0 && node >= 0) {
+        if ((uint32_t)node >= n8 || ++steps > step_cap) {
+          atomicOr(err, (uint32_t)node >= n8 ? KERR_BAD_INDEX : KERR_TIMEOUT);
+          node = -1;
+          gmask = 0;
+          gsp = 0;
+        } else {
+          const float closest = ord_inv((uint32_t)(key_v[lane] >> 32));
+          const int node_idx = node;
+          const float4 *N = bvh8 + 6ll * node;
+          // The 96-byte quantized node in three 256-bit loads: a child's plane
+          // o + q * 2^e is entered at (o - ray.o) / d + q * (2^e / d), one FMA
+          // per plane on the byte q.
+          float4 q0, q1, q2, q3, q4, q5;
+          load_slot8(N, q0, q1);
+          load_slot8(N + 2, q2, q3);
+          load_slot8(N + 4, q4, q5);
+          const uint32_t ew = __float_as_uint(q0.w);
+          const uint32_t fmask = ew >> 24;
+          const float sx = r.ix * pow2i((int)(int8_t)(ew & 0xffu));
+          const float sy = r.iy * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
+          const float sz = r.iz * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
+          const float ax = (q0.x - r.o.x) * r.ix, ay = (q0.y - r.o.y) * r.iy, az = (q0.z - r.o.z) * r.iz;
+          // Near and far byte words per axis (slots 0-3, 4-7): lo for a
+          // positive 1/d, hi for a negative one.
+          const bool fx = (oct & 1u) != 0, fy = (oct & 2u) != 0, fz = (oct & 4u) != 0;
+          const uint32_t lx0 = __float_as_uint(q1.x), lx1 = __float_as_uint(q1.y);
+          const uint32_t ly0 = __float_as_uint(q1.z), ly1 = __float_as_uint(q1.w);
+          const uint32_t lz0 = __float_as_uint(q2.x), lz1 = __float_as_uint(q2.y);
+          const uint32_t hx0 = __float_as_uint(q2.z), hx1 = __float_as_uint(q2.w);
+          const uint32_t hy0 = __float_as_uint(q3.x), hy1 = __float_as_uint(q3.y);
+          const uint32_t hz0 = __float_as_uint(q3.z), hz1 = __float_as_uint(q3.w);
+          const uint32_t nw[6] = {fx ? hx0 : lx0, fx ? hx1 : lx1, fy ? hy0 : ly0,
+                                  fy ? hy1 : ly1, fz ? hz0 : lz0, fz ? hz1 : lz1};
+          const uint32_t fw[6] = {fx ? lx0 : hx0, fx ? lx1 : hx1, fy ? ly0 : hy0,
+                                  fy ? ly1 : hy1, fz ? lz0 : hz0, fz ? lz1 : hz1};
+          ref[0] = __float_as_int(q4.x), ref[1] = __float_as_int(q4.y), ref[2] = __float_as_int(q4.z);
+          ref[3] = __float_as_int(q4.w), ref[4] = __float_as_int(q5.x), ref[5] = __float_as_int(q5.y);
+          ref[6] = __float_as_int(q5.z), ref[7] = __float_as_int(q5.w);
+          uint32_t ibits = 0, nearest = 0;
+          float tbest = INF;
+  #pragma unroll
+          for (int s = 0; s < 8; s++) {
+            const int w = s >> 2, b = s & 3;
+            const float tnx = fmaf(qbyte(nw[0 + w], b), sx, ax), tfx = fmaf(qbyte(fw[0 + w], b), sx, ax);
+            const float tny = fmaf(qbyte(nw[2 + w], b), sy, ay), tfy = fmaf(qbyte(fw[2 + w], b), sy, ay);
+            const float tnz = fmaf(qbyte(nw[4 + w], b), sz, az), tfz = fmaf(qbyte(fw[4 + w], b), sz, az);
+            const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
+            const float tf = min3f(tfx, tfy, fminf(tfz, closest));
+            if (tn <= tf && ((fmask >> s) & 1u)) {
+              if (ref[s] >= 0) {
+                ibits |= 1u << ((uint32_t)s ^ oct);
+                if (tn < tbest) {
+                  tbest = tn;
+                  nearest = (uint32_t)s;
+                }
+              } else {
+                leafmask |= 1u << s;
               }
-            } else {
-              leafmask |= 1u << s;
             }
           }
-        }
-        node = -1;
-        if (ibits) {
-          if (gmask) {
-            if (gsp >= GSTACK) {
-              atomicOr(err, KERR_STACK_OVERFLOW);
-              gsp = 0;
-              gmask = 0;
-              ibits = 0;
-            } else {
-              gstack[gsp++] = (gnode << 8) | gmask;
+          node = -1;
+          if (ibits) {
+            if (gmask) {
+              if (gsp >= GSTACK) {
+                atomicOr(err, KERR_STACK_OVERFLOW);
+                gsp = 0;
+                gmask = 0;
+                ibits = 0;
+              } else {
+                gstack[gsp++] = (gnode << 8) | gmask;
+              }
             }
           }
-        }
-        if (ibits) {
-          // The nearest entered child next; the others later, in rank order.
-          gnode = (uint32_t)node_idx;
-          gmask = ibits & ~(1u << (nearest ^ oct));
-          node = pick8(ref, nearest);
+          if (ibits) {
+            // The nearest entered child next; the others later, in rank order.
+            gnode = (uint32_t)node_idx;
+            gmask = ibits & ~(1u << (nearest ^ oct));
+            node = pick8(ref, nearest);
+          }
         }
       }
-    }
-    // The next entered child of the innermost group, when the lane has no node.
-    if (ray_i >= 0 && node < 0 && (gmask != 0 || gsp > 0)) {
-      if (gmask == 0) {
-        const uint32_t e = gstack[--gsp];
-        gnode = e >> 8;
-        gmask = e & 0xffu;
+      // The next entered child of the innermost group, when the lane has no node.
+      if (ray_i >= 0 && node < 0 && (gmask != 0 || gsp > 0)) {
+        if (gmask == 0) {
+          const uint32_t e = gstack[--gsp];
+          gnode = e >> 8;
+          gmask = e & 0xffu;
+        }
+        const uint32_t rk = (uint32_t)(__ffs(gmask) - 1);
+        gmask &= gmask - 1u;
+        node = __ldg(words8 + 24ll * gnode + 16 + (rk ^ oct));
       }
-      const uint32_t rk = (uint32_t)(__ffs(gmask) - 1);
-      gmask &= gmask - 1u;
-      node = __ldg(words8 + 24ll * gnode + 16 + (rk ^ oct));
-    }
 
-    // Pool this step's leaves (warp-wide exclusive prefix of the counts).
-    const uint32_t c = __popc(leafmask);
-    uint32_t incl = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= (uint32_t)o) incl += y;
-    }
-    const uint32_t added = __shfl_sync(0xffffffffu, incl, 31);
-    if (c) {
-      uint32_t pos = tail + incl - c;
-#pragma unroll
-      for (int s = 0; s < 8; s++) {
-        if (!((leafmask >> s) & 1u)) continue;
-        // Leaf refs were range-checked when the bvh8 was built (k_encode8).
-        pool[pos & (kPool - 1)] = ((uint32_t)~ref[s] << 5) | lane;
-        pos++;
+      // Pool this step's leaves (warp-wide exclusive prefix of the counts).
+      const uint32_t c = __popc(leafmask);
+      uint32_t incl = c;
+  #pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
       }
-      mlp1 = pos;
+      const uint32_t added = __shfl_sync(0xffffffffu, incl, 31);
+      if (c) {
+        uint32_t pos = tail + incl - c;
+  #pragma unroll
+        for (int s = 0; s < 8; s++) {
+          if (!((leafmask >> s) & 1u)) continue;
+          // Leaf refs were range-checked when the bvh8 was built (k_encode8).
+          pool[pos & (kPool - 1)] = ((uint32_t)~ref[s] << 5) | lane;
+          pos++;
+        }
+        mlp1 = pos;
+      }
+      tail += added;
+      __syncwarp();
     }
-    tail += added;
-    __syncwarp();
 
     // Leaf rounds: 32 pooled leaves at a time, oldest first.
     for (;;) {
@@ -650,46 +698,49 @@ inline int cast_block(int b) { return b <= 64 ? 64 : (b >= 256 ? 256 : 128); }
 template <int STACK, int MINB>
 cudaError_t launch_lanes(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
                          uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
-                         int spec, int block, cudaStream_t st) {
+                         int spec, int block, bool refine, cudaStream_t st) {
   auto kern = k_trace_lanes<STACK, MINB>;
   kern<<<persistent_grid(kern, n, block), block, 0, st>>>(sc, rays, n, hits, counter, err, perm, list, list_count,
-                                                           spec);
+                                                           spec, refine);
   return cudaGetLastError();
 }
 
 template <int GSTACK>
 cudaError_t launch_wide(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
                         uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
-                        int minblocks, int refill, int block, cudaStream_t st) {
-  auto kern = minblocks >= 8 ? k_trace_wide<GSTACK, 8, false>
-              : minblocks >= 6 ? k_trace_wide<GSTACK, 6, false>
-                               : k_trace_wide<GSTACK, 5, false>;
-  const size_t smem = (size_t)(block / 32) * kWideWarpSmem;
+                        int minblocks, int refill, int block, int visits, bool refine, cudaStream_t st) {
+  auto kern = visits >= 2 ? (minblocks >= 8   ? k_trace_wide<GSTACK, 8, false, 2>
+                            : minblocks >= 6 ? k_trace_wide<GSTACK, 6, false, 2>
+                                             : k_trace_wide<GSTACK, 5, false, 2>)
+                          : (minblocks >= 8   ? k_trace_wide<GSTACK, 8, false, 1>
+                            : minblocks >= 6 ? k_trace_wide<GSTACK, 6, false, 1>
+                                             : k_trace_wide<GSTACK, 5, false, 1>);
+  const size_t smem = (size_t)(block / 32) * (visits >= 2 ? wide_warp_smem<2>() : wide_warp_smem<1>());
   kern<<<persistent_grid(kern, n, block, smem), block, smem, st>>>(sc, rays, n, nullptr, hits, counter, err, perm,
-                                                                   list, list_count, refill);
+                                                                   list, list_count, refill, refine);
   return cudaGetLastError();
 }
 
 // Group stack of the 8-wide caster: one entry per bvh8 level at most.
 cudaError_t launch_wide_any(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
                             uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
-                            const TraceOpts &opts, cudaStream_t st) {
+                            const TraceOpts &opts, bool refine, cudaStream_t st) {
   const int want = std::max<int>(opts.stack, (int)sc.levels8);
   const int block = cast_block(opts.block);
   if (want <= 16)
     return launch_wide<16>(sc, rays, n, hits, counter, err, perm, list, list_count, opts.wide_minblocks,
-                                   opts.wide_refill, block, st);
+                                   opts.wide_refill, block, opts.wide_visits, refine, st);
   if (want <= 32)
     return launch_wide<32>(sc, rays, n, hits, counter, err, perm, list, list_count, opts.wide_minblocks,
-                                   opts.wide_refill, block, st);
+                                   opts.wide_refill, block, opts.wide_visits, refine, st);
   return launch_wide<64>(sc, rays, n, hits, counter, err, perm, list, list_count, opts.wide_minblocks,
-                                 opts.wide_refill, block, st);
+                                 opts.wide_refill, block, opts.wide_visits, refine, st);
 }
 
 template <int STACK>
 cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
                            uint32_t *err, const TraceOpts &opts, const uint32_t *perm, uint32_t *chunk_scratch,
-                           cudaStream_t st) {
+                           bool refine, cudaStream_t st) {
   const float4 *r4 = reinterpret_cast<const float4 *>(rays);
   int4 *h4 = reinterpret_cast<int4 *>(hits);
   if (opts.refill >= 32) {
@@ -705,25 +756,25 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
                                               : k_trace_packets<STACK, 10>;
       const size_t smem = (size_t)(block / 32) * STACK * sizeof(int);
       pk<<<persistent_grid(pk, n, block, smem), block, smem, st>>>(
-          sc, r4, n, h4, counter, err, perm, opts.defer ? chunk_scratch + 64 : nullptr, chunk_scratch);
+          sc, r4, n, h4, counter, err, perm, opts.defer ? chunk_scratch + 64 : nullptr, chunk_scratch, refine);
       if (!opts.defer) return cudaGetLastError();
       list = chunk_scratch + 64;
       list_count = chunk_scratch;
       lane_counter = chunk_scratch + 1;
     }
     if (use_wide(opts, sc))
-      return launch_wide_any(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts, st);
+      return launch_wide_any(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts, refine, st);
     if (opts.minblocks >= 16)
       return launch_lanes<STACK, 16>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec,
-                                             block, st);
+                                             block, refine, st);
     if (opts.minblocks >= 12)
       return launch_lanes<STACK, 12>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec,
-                                             block, st);
+                                             block, refine, st);
     return launch_lanes<STACK, 10>(sc, r4, n, h4, lane_counter, err, perm, list, list_count, opts.spec,
-                                           block, st);
+                                           block, refine, st);
   }
   auto kt = k_trace<STACK>;
-  kt<<<persistent_grid(kt, n), kTraceBlock, 0, st>>>(sc, r4, n, h4, counter, err, opts.refill, perm);
+  kt<<<persistent_grid(kt, n), kTraceBlock, 0, st>>>(sc, r4, n, h4, counter, err, opts.refill, perm, refine);
   return cudaGetLastError();
 }
 
@@ -744,18 +795,18 @@ cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t ca
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
   const float4 *r4 = reinterpret_cast<const float4 *>(rays);
-  const size_t smem = (size_t)(kTraceBlock / 32) * kWideWarpSmem;
+  const size_t smem = (size_t)(kTraceBlock / 32) * wide_warp_smem<1>();
   auto go = [&](auto kern) {
     kern<<<persistent_grid(kern, cap, kTraceBlock, smem), kTraceBlock, smem, st>>>(sc, r4, cap, d_n, hits, counter,
                                                                                    err, perm, list, list_count,
-                                                                                   refill);
+                                                                                   refill, false);
     return cudaGetLastError();
   };
   if (sc.levels8 <= 16)
-    return minblocks >= 8 ? go(k_trace_wide<16, 8, true>) : go(k_trace_wide<16, 6, true>);
+    return minblocks >= 8 ? go(k_trace_wide<16, 8, true, 1>) : go(k_trace_wide<16, 6, true, 1>);
   if (sc.levels8 <= 32)
-    return minblocks >= 8 ? go(k_trace_wide<32, 8, true>) : go(k_trace_wide<32, 6, true>);
-  return minblocks >= 8 ? go(k_trace_wide<64, 8, true>) : go(k_trace_wide<64, 6, true>);
+    return minblocks >= 8 ? go(k_trace_wide<32, 8, true, 1>) : go(k_trace_wide<32, 6, true, 1>);
+  return minblocks >= 8 ? go(k_trace_wide<64, 8, true, 1>) : go(k_trace_wide<64, 6, true, 1>);
 }
 
 size_t trace_chunk_scratch_bytes(uint32_t n) { return 4ull * (64 + (n + 31) / 32); }
@@ -775,16 +826,9 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
   // Traversal stack: trace.stack entries (16, 32 or 64), raised to the
   // smallest size that holds the tree's depth.
   const int stk = trace_stack_entries(opts, sc);
-  e = stk <= 16   ? launch_variant<16>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st)
-      : stk <= 32 ? launch_variant<32>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st)
-                  : launch_variant<64>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, st);
-  if (e != cudaSuccess || !refine) return e;
-  // The chosen triangles' t, u, v again in fp64, one converged pass over
-  // the batch (inside the casters the per-lane finish is divergent, and a
-  // lone lane's fp64 work costs the whole warp's pipe time).
-  k_refine_hits<<<(n + 255) / 256, 256, 0, st>>>(sc.tris, sc.ntris, reinterpret_cast<const float4 *>(rays), n,
-                                                 reinterpret_cast<int4 *>(hits));
-  return cudaGetLastError();
+  return stk <= 16   ? launch_variant<16>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, refine, st)
+         : stk <= 32 ? launch_variant<32>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, refine, st)
+                     : launch_variant<64>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, refine, st);
 }
 
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
