@@ -66,7 +66,7 @@ double rtgbUniform(uint64_t seed, uint64_t index);
  * of which the slots set in `fmask` (bit s: slot s, at least one) are
  * filled; `out` receives the node's 24 words (origin, int8 exponents and
  * the filled mask, 8-bit child bounds with qlo = 255, qhi = 0 in empty
- * slots, refs with INT_MIN in empty slots). Returns 1, or 0 when a box
+ * slots, refs with ~0 in empty slots). Returns 1, or 0 when a box
  * does not fit the node's grid. Exposed so the decoded boxes can be checked
  * to contain the originals without a GPU. */
 uint32_t rtgbQuantizeNode8(const float *boxes, const int32_t *refs, uint32_t fmask, uint32_t *out);

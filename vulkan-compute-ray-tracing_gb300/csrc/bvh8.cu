@@ -29,11 +29,16 @@
 //   words 4-15   8-bit child bounds qlo.x[8], qlo.y, qlo.z, qhi.x, qhi.y,
 //                qhi.z (slot s in byte s & 3 of word 2 * plane + (s >> 2));
 //                an empty slot has qlo = 255, qhi = 0
-//   words 16-23  child refs
+//   words 16-23  child refs; an empty slot holds ~0 (the leaf of tpre
+//                record 0)
 // A child's box decodes to o + q * 2^e per axis. qlo is rounded down and
 // qhi up, and both are checked against the fp32 box, so the decoded box
 // always contains the original one. Refs: >= 0 is an inner child (its node
-// number); ~k is a leaf (tpre record k, as in bvh2); INT_MIN an empty slot.
+// number); ~k is a leaf (tpre record k, as in bvh2). An empty slot's
+// inverted box misses every ray whose 1/d is not flushed to zero on all
+// three axes; should one still pass, its ref sends the lane to test record
+// 0, a real triangle, which cannot change a closest hit. The traversal
+// therefore needs no filled-mask test per slot.
 // Nodes are numbered breadth first, level by level; the inner children of
 // one node are consecutive, in slot order.
 #include <cuda_runtime.h>
@@ -53,7 +58,8 @@ namespace rtgb {
 // becomes a byte, rounded down for lo and up for hi, then checked in fp64
 // against the fp32 bound and moved outward if needed, so the decoded box
 // o + q * 2^e always contains the original. Empty slots get qlo = 255,
-// qhi = 0. False when some box does not fit the grid (or fmask is empty).
+// qhi = 0 and ref ~0. False when some box does not fit the grid (or fmask is
+// empty).
 __host__ __device__ inline bool quantize_node8(const float box[8][6], const int32_t ref[8], uint32_t fmask,
                                                uint32_t w[24]) {
   fmask &= 0xffu;
@@ -104,7 +110,7 @@ __host__ __device__ inline bool quantize_node8(const float box[8][6], const int3
     ebytes |= ((uint32_t)(e & 0xff)) << (8 * k);
   }
   w[3] = ebytes;
-  for (int s = 0; s < 8; s++) w[16 + s] = (uint32_t)ref[s];
+  for (int s = 0; s < 8; s++) w[16 + s] = (fmask >> s) & 1u ? (uint32_t)ref[s] : ~0u;
   return ok;
 }
 

@@ -46,7 +46,7 @@ __device__ __forceinline__ int traverse_literal16(const DevScene &sc, f3 o, f3 d
       f3 a = sub3(v0, v1), b = sub3(v2, v0);
       f3 n = cross3(b, a);
       f3 p = sub3(v0, o);
-      float idet = __fdiv_rn(1.0f, dot3(d, n));
+      float idet = __frcp_rn(dot3(d, n));  // correctly rounded 1/x: the value of the IEEE division 1.0f / x
       float t = __fmul_rn(dot3(n, p), idet);
       f3 q = cross3(p, d);
       float u = __fmul_rn(dot3(q, b), idet);

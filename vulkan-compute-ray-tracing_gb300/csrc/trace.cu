@@ -311,7 +311,7 @@ __device__ __forceinline__ bool tri_candidate(const float4 *__restrict__ tpre, i
   const f3 v0 = mk3(t0.x, t0.y, t0.z), n = mk3(t0.w, t1.x, t1.y);
   const f3 a = mk3(t1.z, t1.w, t2.x), b = mk3(t2.y, t2.z, t2.w);
   const f3 p = sub3(v0, o);
-  const float idet = __fdiv_rn(1.0f, dot3(d, n));
+  const float idet = __frcp_rn(dot3(d, n));  // correctly rounded 1/x: the value of the IEEE division 1.0f / x
   t = __fmul_rn(dot3(n, p), idet);
   if (!(t > tmin && t <= closest)) return false;
   const f3 q = cross3(p, d);
@@ -354,7 +354,8 @@ __device__ __forceinline__ int32_t pick8(const int32_t (&ref)[8], uint32_t s) {
 // loads) and tests its eight slots. Each axis's near and far planes are
 // picked once per node by the sign of the lane's 1/d (a select on the byte
 // words), so a slot costs six byte decodes, six FMAs and two three-operand
-// min/max; the filled mask drops empty slots. The node's slots were
+// min/max; empty slots hold an inverted box (and a harmless leaf ref), so
+// no per-slot mask test is needed. The node's slots were
 // assigned by octant (bvh8.cu), so the entered inner children, kept as the
 // bits s ^ o of a rank mask (o: the sign bits of the ray's direction), come
 // out roughly near-first by taking the lowest set bit — no distance sort.
@@ -533,8 +534,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
           load_slot8(N + 2, q2, q3);
           load_slot8(N + 4, q4, q5);
           const uint32_t ew = __float_as_uint(q0.w);
-          const uint32_t fmask = ew >> 24;
-          const float sx = r.ix * pow2i((int)(int8_t)(ew & 0xffu));
+            const float sx = r.ix * pow2i((int)(int8_t)(ew & 0xffu));
           const float sy = r.iy * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
           const float sz = r.iz * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
           const float ax = (q0.x - r.o.x) * r.ix, ay = (q0.y - r.o.y) * r.iy, az = (q0.z - r.o.z) * r.iz;
@@ -564,7 +564,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
             const float tnz = fmaf(qbyte(nw[4 + w], b), sz, az), tfz = fmaf(qbyte(fw[4 + w], b), sz, az);
             const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
             const float tf = min3f(tfx, tfy, fminf(tfz, closest));
-            if (tn <= tf && ((fmask >> s) & 1u)) {
+            if (tn <= tf) {
               if (ref[s] >= 0) {
                 ibits |= 1u << ((uint32_t)s ^ oct);
                 if (tn < tbest) {

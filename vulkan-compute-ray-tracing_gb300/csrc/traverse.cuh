@@ -130,7 +130,7 @@ __device__ __forceinline__ void test_triangle(const float4 *__restrict__ tpre, c
   f3 v0 = mk3(t0.x, t0.y, t0.z), n = mk3(t0.w, t1.x, t1.y);
   f3 a = mk3(t1.z, t1.w, t2.x), b = mk3(t2.y, t2.z, t2.w);
   f3 p = sub3(v0, r.o);
-  float idet = __fdiv_rn(1.0f, dot3(r.d, n));
+  float idet = __frcp_rn(dot3(r.d, n));  // correctly rounded 1/x: the value of the IEEE division 1.0f / x
   float t = __fmul_rn(dot3(n, p), idet);
   if (t > r.tmin &&
       (t < closest || (t == closest && best >= 0 && __ldg(leaf_tri + k) < __ldg(leaf_tri + best)))) {
