@@ -57,6 +57,9 @@ WORKLOAD = "closest-hit, icosphere L8 (1,310,720 tris), 4,194,304 coherent + 4,1
 ALG_BYTES_COHERENT = 48.0 * (530.158 + 61.469) + 48.0
 ALG_BYTES_INCOHERENT = 48.0 * (370.590 + 41.355) + 48.0
 RAYS_PER_BATCH = 2048 * 2048
+TUNING_KEYS = ("trace.block", "trace.stack", "trace.sort", "trace.packet", "trace.packet_minblocks", "trace.defer",
+               "trace.wide", "trace.wide_minblocks", "trace.wide_visits", "trace.wide_refill", "trace.minblocks",
+               "trace.spec")
 
 
 def measured_peak_hbm():
@@ -405,6 +408,7 @@ def run_gpu(args):
         return
     clocks = clk.summary()
     sm_mhz = clocks.get("sm_mhz") or 2070.0
+    tuning = {k: ctx.get_tuning(k) for k in TUNING_KEYS}
     per = [kernel_roofline("k_trace_packets", coh_ms, ALG_BYTES_COHERENT, sm_mhz),
            kernel_roofline("k_trace_wide", inc_ms, ALG_BYTES_INCOHERENT, sm_mhz)]
     dom = max(per, key=lambda e: e["batch_ms"])
@@ -432,6 +436,9 @@ def run_gpu(args):
         # Per batch: 7 reordering kernels (extent, histogram, 3-kernel scan,
         # scatter, init) + 2 casting kernels (packets, then the listed
         # chunks per lane); two batches per step.
+        # Launch shape the casts ran with (rtSetTuning keys; the defaults,
+        # which rtAutotuneTrace keeps on this workload).
+        "tuning": tuning,
         "gpu_launches": 18 * args.steps,
         "clocks": clocks,
     }

@@ -191,13 +191,13 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   boxes of a node, and leaves are tested 32 at a time by
  *                   the whole warp from a shared pool; 0 = the binary layout
  *                   with postponed leaves. Results are identical either way
- *   "trace.wide_minblocks" 8, 6 (default) or 5: resident 128-thread blocks
+ *   "trace.wide_minblocks" 8, 7, 6 (default) or 5: resident 128-thread blocks
  *                   per SM the 8-wide caster is compiled for
  *   "trace.wide_refill"  idle lanes of an 8-wide caster warp that trigger
  *                   a fetch of new rays (1..32, default 4)
  *   "trace.wide_visits"  node steps a lane of the 8-wide caster takes per
  *                   loop iteration before the warp's shared leaf pool and
- *                   refill bookkeeping run (1, or 2 default)
+ *                   refill bookkeeping run (1, 2 or 3, default 3)
  *   "trace.wide_min_tris"  scenes with at least this many triangles use
  *                   the 8-wide caster (default 2^17; smaller trees stay in
  *                   cache, where the binary layout is faster); it applies

@@ -365,7 +365,7 @@ def test_autotune_trace_keeps_hits(rt, orc, ctx):
         d_hits = torch.zeros((len(rays), 4), dtype=torch.float32, device="cuda")
         before, after = rt.autotune_trace(sc, d_rays, len(rays), d_hits, reps=1)
         assert before > 0 and after > 0
-        allowed = {"trace.wide_minblocks": (8, 6, 5), "trace.minblocks": (16, 12, 10), "trace.wide_visits": (1, 2),
+        allowed = {"trace.wide_minblocks": (8, 7, 6, 5), "trace.minblocks": (16, 12, 10), "trace.wide_visits": (1, 2, 3),
                    "trace.packet_minblocks": (16, 12, 10), "trace.block": (64, 128, 256),
                    "trace.stack": (0, 32, 64)}
         for k in keys:
@@ -400,7 +400,7 @@ def test_block_size_and_stack_depth_keep_hits(rt, ctx, level, wide_min):
             for stack in (0, 16, 32, 64):
                 ctx.set_tuning("trace.block", block)
                 ctx.set_tuning("trace.stack", stack)
-                ctx.set_tuning("trace.wide_visits", 2 if stack % 32 else 1)
+                ctx.set_tuning("trace.wide_visits", 1 + (stack // 16) % 3)
                 got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
                 assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (block, stack)
                 # The default (fp64 re-evaluated) results agree as well.

@@ -767,7 +767,7 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     return RT_SUCCESS;
   }
   if (k == "trace.wide_minblocks") {
-    if (value != 8 && value != 6 && value != 5) return RT_ERR_INVALID_ARGUMENT;
+    if (value < 5 || value > 8) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.wide_minblocks = (int)value;
     return RT_SUCCESS;
   }
@@ -782,7 +782,7 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     return RT_SUCCESS;
   }
   if (k == "trace.wide_visits") {
-    if (value != 1 && value != 2) return RT_ERR_INVALID_ARGUMENT;
+    if (value < 1 || value > 3) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.wide_visits = (int)value;
     return RT_SUCCESS;
   }

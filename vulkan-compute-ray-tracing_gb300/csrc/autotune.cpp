@@ -93,8 +93,8 @@ rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, 
   const Knob knobs[] = {{"trace.block", {128, 64, 256}},
                         {"trace.stack", {0, 32, 64}},
                         {"trace.wide", {1, 0}},
-                        {"trace.wide_minblocks", {8, 6, 5}},
-                        {"trace.wide_visits", {2, 1}},
+                        {"trace.wide_minblocks", {8, 7, 6, 5}},
+                        {"trace.wide_visits", {3, 2, 1}},
                         {"trace.defer", {1, 0}},
                         {"trace.spec", {1, 0}},
                         {"trace.minblocks", {16, 12, 10}},

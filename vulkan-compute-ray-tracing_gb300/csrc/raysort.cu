@@ -52,7 +52,11 @@ __device__ __forceinline__ void ray_coords(const float4 *rays, uint32_t i, float
   octa(b.x, b.y, b.z, c[3], c[4]);
 }
 
-// ext[0..4] = ordered min, ext[5..9] = ordered max (initialised by the host).
+// ext[0..4] = ordered min, ext[5..9] = ordered max (initialised by the host),
+// over one ray in kExtentStride: the extent only scales the Morton key, and
+// rays outside the sampled extent clamp to the edge buckets (the order only
+// affects speed, never results), so the pass reads an eighth of the rays.
+constexpr uint32_t kExtentStride = 8;
 __global__ void k_extent(const float4 *__restrict__ rays, uint32_t n, const uint32_t *d_n, uint32_t *ext) {
   if (d_n) n = min(n, *d_n);
   float lo[5], hi[5];
@@ -60,7 +64,8 @@ __global__ void k_extent(const float4 *__restrict__ rays, uint32_t n, const uint
     lo[k] = __int_as_float(0x7f800000);
     hi[k] = -__int_as_float(0x7f800000);
   }
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (uint64_t i = (uint64_t)(blockIdx.x * blockDim.x + threadIdx.x) * kExtentStride; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x * kExtentStride) {
     float c[5];
     ray_coords(rays, i, c);
     for (int k = 0; k < 5; k++) {

@@ -330,7 +330,7 @@ __device__ __forceinline__ float qbyte(uint32_t w, int b) {
 
 // Leaf pool entries per warp (power of two): at most 31 are left after the
 // leaf rounds of an iteration, and each of its VISITS node steps adds at
-// most 8 per lane.
+// most 8 per lane (31 + 3 * 256 < 1024).
 template <int VISITS>
 __host__ __device__ constexpr int pool_entries() {
   return VISITS == 1 ? 512 : 1024;
@@ -709,13 +709,20 @@ template <int GSTACK>
 cudaError_t launch_wide(const DevScene &sc, const float4 *rays, uint32_t n, int4 *hits, uint32_t *counter,
                         uint32_t *err, const uint32_t *perm, const uint32_t *list, const uint32_t *list_count,
                         int minblocks, int refill, int block, int visits, bool refine, cudaStream_t st) {
-  auto kern = visits >= 2 ? (minblocks >= 8   ? k_trace_wide<GSTACK, 8, false, 2>
+  auto kern = visits >= 3 ? (minblocks >= 8   ? k_trace_wide<GSTACK, 8, false, 3>
+                            : minblocks >= 7 ? k_trace_wide<GSTACK, 7, false, 3>
+                            : minblocks >= 6 ? k_trace_wide<GSTACK, 6, false, 3>
+                                             : k_trace_wide<GSTACK, 5, false, 3>)
+            : visits >= 2 ? (minblocks >= 8   ? k_trace_wide<GSTACK, 8, false, 2>
+                            : minblocks >= 7 ? k_trace_wide<GSTACK, 7, false, 2>
                             : minblocks >= 6 ? k_trace_wide<GSTACK, 6, false, 2>
                                              : k_trace_wide<GSTACK, 5, false, 2>)
                           : (minblocks >= 8   ? k_trace_wide<GSTACK, 8, false, 1>
+                            : minblocks >= 7 ? k_trace_wide<GSTACK, 7, false, 1>
                             : minblocks >= 6 ? k_trace_wide<GSTACK, 6, false, 1>
                                              : k_trace_wide<GSTACK, 5, false, 1>);
   const size_t smem = (size_t)(block / 32) * (visits >= 2 ? wide_warp_smem<2>() : wide_warp_smem<1>());
+  static_assert(wide_warp_smem<3>() == wide_warp_smem<2>(), "visits 2 and 3 share the pool size");
   kern<<<persistent_grid(kern, n, block, smem), block, smem, st>>>(sc, rays, n, nullptr, hits, counter, err, perm,
                                                                    list, list_count, refill, refine);
   return cudaGetLastError();
