@@ -24,8 +24,9 @@ enum : uint32_t {
 // Traversal layout (derived on the GPU from `nodes`):
 //   bvh2    4 x float4 per inner node (64 B): the boxes of both children,
 //           x/y slabs of child 0 and child 1, then the z slabs of both,
-//           then (ref0, ref1). ref >= 0 is an inner node, ref < 0 is the
-//           leaf ~k whose triangle is tpre[k].
+//           then (ref0, ref1, order, 0). ref >= 0 is an inner node, ref < 0
+//           is the leaf ~k whose triangle is tpre[k]; bit o of `order` set:
+//           child 1 is visited first by rays of sign octant o.
 //   tpre    3 x float4 per triangle in leaf order (48 B): v0, n = cross(b, a),
 //           a = v0 - v1, b = v2 - v0 — the per-triangle terms of triIntersect
 //           (ray-trace-compute.comp:157-173), computed once with the same

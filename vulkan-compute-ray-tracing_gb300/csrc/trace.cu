@@ -121,16 +121,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
         const float4 *N = bvh + 4ll * node;
         float4 a, b, c, d;
         load_node(N, a, b, c, d);
-        float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-        float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+        const bool h0 = slab_hit(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+        const bool h1 = slab_hit(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
         int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
-        bool h0 = t0 < __int_as_float(0x7f800000), h1 = t1 < __int_as_float(0x7f800000);
         if (h0 && h1) {
-          int nearc = r0, farc = r1;
-          if (t1 < t0) {
-            nearc = r1;
-            farc = r0;
-          }
+          const bool f1 = child1_first(d, ray_octant(r));
+          const int nearc = f1 ? r1 : r0, farc = f1 ? r0 : r1;
           if (sp >= STACK) {
             atomicOr(err, KERR_STACK_OVERFLOW);
             node = kDone;

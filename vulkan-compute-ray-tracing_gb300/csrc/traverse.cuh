@@ -80,12 +80,11 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // for i > 0 because rounding is monotonic, so min/max pick exactly those
 // values. The fixed form saves six ALU operations per box.
 template <int OCT = -1>
-__device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float hx, float ly, float hy, float lz,
-                                            float hz, float tmax) {
+__device__ __forceinline__ void slab_span(const TraceRay &r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                          float tmax, float &tn, float &tf) {
   float ax = fmaf(lx, r.ix, -r.ox), bx = fmaf(hx, r.ix, -r.ox);
   float ay = fmaf(ly, r.iy, -r.oy), by = fmaf(hy, r.iy, -r.oy);
   float az = fmaf(lz, r.iz, -r.oz), bz = fmaf(hz, r.iz, -r.oz);
-  float tn, tf;
   if (OCT < 0) {
     tn = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), r.tmin));
     tf = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
@@ -96,8 +95,29 @@ __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float h
     tn = max3f(nx, ny, fmaxf(nz, r.tmin));
     tf = min3f(fx, fy, fminf(fz, tmax));
   }
+}
+
+template <int OCT = -1>
+__device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float hx, float ly, float hy, float lz,
+                                            float hz, float tmax) {
+  float tn, tf;
+  slab_span<OCT>(r, lx, hx, ly, hy, lz, hz, tmax, tn, tf);
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
+
+// The same test as a flag, for loops that order children without distances.
+template <int OCT = -1>
+__device__ __forceinline__ bool slab_hit(const TraceRay &r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                         float tmax) {
+  float tn, tf;
+  slab_span<OCT>(r, lx, hx, ly, hy, lz, hz, tmax, tn, tf);
+  return tn <= tf;
+}
+
+// Near-first order at a pair node: true when child 1 is visited first by
+// rays of sign octant `oct` (the node's order bits, relayout.cu). Any order
+// gives the same hit; this one needs no entry distance.
+__device__ __forceinline__ bool child1_first(float4 d, int oct) { return (__float_as_uint(d.z) >> oct) & 1u; }
 
 // Sign octant of the ray's inverse direction (the OCT of slab_enter).
 __device__ __forceinline__ int ray_octant(const TraceRay &r) {
@@ -159,22 +179,19 @@ __device__ __forceinline__ int traverse_closest_on(const DevScene &sc, const Tra
   if (!(root < __int_as_float(0x7f800000))) return -1;
   int sp = 0;
   int node = sc.root_ref;
+  const int oct = ray_octant(r);
   const float4 *__restrict__ bvh = sc.bvh2;
   for (;;) {
     while (node >= 0) {
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      float t0 = slab_enter(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      float t1 = slab_enter(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      const bool h0 = slab_hit(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+      const bool h1 = slab_hit(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
       int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
-      bool h0 = t0 < __int_as_float(0x7f800000), h1 = t1 < __int_as_float(0x7f800000);
       if (h0 && h1) {
-        int nearc = r0, farc = r1;
-        if (t1 < t0) {
-          nearc = r1;
-          farc = r0;
-        }
+        const bool f1 = child1_first(d, oct);
+        const int nearc = f1 ? r1 : r0, farc = f1 ? r0 : r1;
         if (sp >= STACK) {
           atomicOr(err, KERR_STACK_OVERFLOW);
           return best;
@@ -227,6 +244,7 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
                             sc.root_hi[2], closest);
     if (root < __int_as_float(0x7f800000)) node = sc.root_ref;
   }
+  const int oct = OCT >= 0 ? OCT : ray_octant(r);
   const float4 *__restrict__ bvh = sc.bvh2;
   while (node != kEnd || leaf < 0) {
     // A leaf in hand and none parked (only when the root is a leaf).
@@ -238,16 +256,12 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      float t0 = slab_enter<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      float t1 = slab_enter<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      const bool h0 = slab_hit<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
+      const bool h1 = slab_hit<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
       int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
-      bool h0 = t0 < __int_as_float(0x7f800000), h1 = t1 < __int_as_float(0x7f800000);
       if (h0 && h1) {
-        int nearc = r0, farc = r1;
-        if (t1 < t0) {
-          nearc = r1;
-          farc = r0;
-        }
+        const bool f1 = child1_first(d, oct);
+        const int nearc = f1 ? r1 : r0, farc = f1 ? r0 : r1;
         if (sp >= STACK) {
           atomicOr(err, KERR_STACK_OVERFLOW);
           return best;
@@ -301,8 +315,8 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
 // is exactly its per-ray closest hit (the packet visits a superset of every
 // lane's required nodes); only the number of visited nodes changes.
 // Inactive lanes carry closest = -inf, so they miss every box and accept no
-// triangle without extra tests. Near/far order follows the first active
-// lane. The stack is warp-distributed in registers for STACK <= 32 (entry j
+// triangle without extra tests. Near/far order comes from the node's order
+// bits for the packet's octant. The stack is warp-distributed in registers for STACK <= 32 (entry j
 // in lane j, read back with a shuffle), else in shared memory. All branches
 // are warp-uniform except inside the triangle test.
 template <int STACK, int OCT = -1>
@@ -326,24 +340,26 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
   int sp = 0;
   int node = sc.root_ref;
   int reg_stack = 0;  // entry `lane` of the register stack (STACK <= 32)
+  // The packet's octant (the first active lane's for a mixed warp) picks
+  // the near child from the node's order bits.
+  const int oct = OCT >= 0 ? OCT : __shfl_sync(0xffffffffu, ray_octant(r), src);
+  const uint32_t ref_span = 2u * sc.ntris - 1u;
   const float4 *__restrict__ bvh = sc.bvh2;
   for (;;) {
     if (node >= 0) {
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      float t0 = slab_enter<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      float t1 = slab_enter<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
-      const uint32_t m0 = __ballot_sync(0xffffffffu, t0 < INF), m1 = __ballot_sync(0xffffffffu, t1 < INF);
+      const bool any0 = __any_sync(0xffffffffu, slab_hit<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest));
+      const bool any1 = __any_sync(0xffffffffu, slab_hit<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest));
       const int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
-      if (m0 && m1) {
-        // The first active lane's order; a lane that misses a child ranks it last.
-        const bool first0 = __shfl_sync(0xffffffffu, t0 <= t1, src);
+      if (any0 && any1) {
+        const bool f1 = child1_first(d, oct);
         if (sp >= STACK) {
           if (lane == 0) atomicOr(err, KERR_STACK_OVERFLOW);
           break;
         }
-        const int farc = first0 ? r1 : r0;
+        const int farc = f1 ? r0 : r1;
         if (STACK <= 32) {
           if (lane == (uint32_t)sp) reg_stack = farc;
         } else {
@@ -351,12 +367,12 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
           __syncwarp();
         }
         sp++;
-        node = first0 ? r0 : r1;
+        node = f1 ? r1 : r0;
         continue;
-      } else if (m0) {
+      } else if (any0) {
         node = r0;
         continue;
-      } else if (m1) {
+      } else if (any1) {
         node = r1;
         continue;
       }
@@ -366,8 +382,9 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
     if (sp == 0) break;
     --sp;
     node = STACK <= 32 ? __shfl_sync(0xffffffffu, reg_stack, sp) : stack[sp];
-    // A popped ref is an inner node (< ntris - 1) or a leaf ~k (k < ntris).
-    if (node >= (int)sc.ntris - 1 || node < -(int)sc.ntris) {
+    // A popped ref is an inner node (< ntris - 1) or a leaf ~k (k < ntris):
+    // node + ntris lies in [0, 2 ntris - 1).
+    if ((uint32_t)node + sc.ntris >= ref_span) {
       if (lane == 0) atomicOr(err, KERR_BAD_INDEX);
       break;
     }
