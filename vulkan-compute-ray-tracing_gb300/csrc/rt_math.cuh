@@ -48,6 +48,40 @@ __device__ __forceinline__ f3 cross3(f3 a, f3 b) {
 __device__ __forceinline__ float length3(f3 a) { return __fsqrt_rn(dot3(a, a)); }
 // normalize(v) = v / length(v), one IEEE division per component.
 __device__ __forceinline__ f3 normalize3(f3 a) { return divs3(a, length3(a)); }
+
+// Two fp32 values in one 64-bit register pair, for the packed arithmetic of
+// sm_100 and later (add/mul/fma .f32x2): one instruction computes both
+// halves, each rounded exactly as the scalar operation with the same
+// rounding mode would round it.
+struct f2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ f2 pk2(float lo, float hi) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float lo2(f2 a) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+  return lo;
+}
+__device__ __forceinline__ float hi2(f2 a) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+  return hi;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.v) : "l"(a.v), "l"(b.v));
+  return d;
+}
+
 // GLSL min/max in the specification's wording.
 __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
 __device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }

@@ -318,10 +318,20 @@ __device__ __forceinline__ bool tri_candidate(const float4 *__restrict__ tpre, i
 
 // 2^e as fp32 for e in [-126, 127].
 __device__ __forceinline__ float pow2i(int e) { return __int_as_float((e + 127) << 23); }
-// Byte b of w as fp32, exactly: 2^23 + byte assembled by a byte permute, then
-// 2^23 subtracted.
-__device__ __forceinline__ float qbyte(uint32_t w, int b) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)b)) - 8388608.0f;
+// Byte b of w as the fp32 value 2^23 + byte (exact), assembled by a byte
+// permute; the caster subtracts 2^23 from two such values with one packed
+// instruction, which gives the byte exactly.
+__device__ __forceinline__ float qraw(uint32_t w, int b) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)b));
+}
+
+// Slot-order bits to rank order: bit s moves to bit s ^ oct (three
+// conditional swaps of bit groups).
+__device__ __forceinline__ uint32_t rank_bits(uint32_t x, uint32_t oct) {
+  if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+  if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+  if (oct & 4u) x = ((x & 0x0fu) << 4) | ((x >> 4) & 0x0fu);
+  return x;
 }
 
 // Leaf pool entries per warp (power of two): at most 31 are left after the
@@ -421,6 +431,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
     fhead += cnt;
   };
   const float INF = __int_as_float(0x7f800000);
+  const f2 qbias2 = pk2(8388608.0f, 8388608.0f);  // the 2^23 of qraw, twice
   if (d_n) n = min(n, *d_n);
   const uint32_t total = list ? min(*list_count, (n + 31) / 32) * 32u : n;
   const float4 *__restrict__ bvh8 = sc.bvh8;
@@ -550,28 +561,35 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
           ref[0] = __float_as_int(q4.x), ref[1] = __float_as_int(q4.y), ref[2] = __float_as_int(q4.z);
           ref[3] = __float_as_int(q4.w), ref[4] = __float_as_int(q5.x), ref[5] = __float_as_int(q5.y);
           ref[6] = __float_as_int(q5.z), ref[7] = __float_as_int(q5.w);
-          uint32_t ibits = 0, nearest = 0;
-          float tbest = INF;
+          // Per slot and axis, the near and far planes in one packed FMA on
+          // the pair of exact byte values (2^23 + q assembled by a byte
+          // permute, 2^23 subtracted). The nearest entered inner child is
+          // the minimum of keys (entry distance with its low three bits
+          // replaced by the slot), an order within 8 ulps of the distances.
+          const f2 sxx = pk2(sx, sx), syy = pk2(sy, sy), szz = pk2(sz, sz);
+          const f2 axx = pk2(ax, ax), ayy = pk2(ay, ay), azz = pk2(az, az);
+          uint32_t hin = 0;
+          float kbest = INF;
   #pragma unroll
           for (int s = 0; s < 8; s++) {
             const int w = s >> 2, b = s & 3;
-            const float tnx = fmaf(qbyte(nw[0 + w], b), sx, ax), tfx = fmaf(qbyte(fw[0 + w], b), sx, ax);
-            const float tny = fmaf(qbyte(nw[2 + w], b), sy, ay), tfy = fmaf(qbyte(fw[2 + w], b), sy, ay);
-            const float tnz = fmaf(qbyte(nw[4 + w], b), sz, az), tfz = fmaf(qbyte(fw[4 + w], b), sz, az);
-            const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
-            const float tf = min3f(tfx, tfy, fminf(tfz, closest));
+            const f2 tx = fma2(sub2(pk2(qraw(nw[0 + w], b), qraw(fw[0 + w], b)), qbias2), sxx, axx);
+            const f2 ty = fma2(sub2(pk2(qraw(nw[2 + w], b), qraw(fw[2 + w], b)), qbias2), syy, ayy);
+            const f2 tz = fma2(sub2(pk2(qraw(nw[4 + w], b), qraw(fw[4 + w], b)), qbias2), szz, azz);
+            const float tn = max3f(lo2(tx), lo2(ty), fmaxf(lo2(tz), r.tmin));
+            const float tf = min3f(hi2(tx), hi2(ty), fminf(hi2(tz), closest));
             if (tn <= tf) {
               if (ref[s] >= 0) {
-                ibits |= 1u << ((uint32_t)s ^ oct);
-                if (tn < tbest) {
-                  tbest = tn;
-                  nearest = (uint32_t)s;
-                }
+                hin |= 1u << s;
+                kbest = fminf(kbest, __uint_as_float((__float_as_uint(tn) & ~7u) | (uint32_t)s));
               } else {
                 leafmask |= 1u << s;
               }
             }
           }
+          // An infinite entry distance leaves no usable key: take the lowest slot.
+          const uint32_t nearest = kbest < INF ? (__float_as_uint(kbest) & 7u) : (uint32_t)(__ffs(hin) - 1);
+          uint32_t ibits = rank_bits(hin, oct);
           node = -1;
           if (ibits) {
             if (gmask) {
