@@ -171,8 +171,8 @@ __device__ __forceinline__ float slot_area(const Slot &s) {
 __device__ __forceinline__ void load_pair(const float4 *__restrict__ bvh2, int32_t p, Slot &c0, Slot &c1) {
   const float4 *N = bvh2 + 4ll * p;
   const float4 a = N[0], b = N[1], c = N[2], d = N[3];
-  c0.lo[0] = a.x, c0.hi[0] = a.y, c0.lo[1] = a.z, c0.hi[1] = a.w, c0.lo[2] = c.x, c0.hi[2] = c.y;
-  c1.lo[0] = b.x, c1.hi[0] = b.y, c1.lo[1] = b.z, c1.hi[1] = b.w, c1.lo[2] = c.z, c1.hi[2] = c.w;
+  c0.lo[0] = a.x, c0.lo[1] = a.y, c0.hi[0] = a.z, c0.hi[1] = a.w, c0.lo[2] = c.x, c0.hi[2] = c.y;
+  c1.lo[0] = b.x, c1.lo[1] = b.y, c1.hi[0] = b.z, c1.hi[1] = b.w, c1.lo[2] = c.z, c1.hi[2] = c.w;
   c0.ref = __float_as_int(d.x);
   c1.ref = __float_as_int(d.y);
 }

@@ -23,7 +23,8 @@ enum : uint32_t {
 //   nodes   rt_bvh_node[nnodes]  48 B, nnodes = 2*ntris - 1
 // Traversal layout (derived on the GPU from `nodes`):
 //   bvh2    4 x float4 per inner node (64 B): the boxes of both children,
-//           x/y slabs of child 0 and child 1, then the z slabs of both,
+//           (lo.x, lo.y, hi.x, hi.y) of child 0 and of child 1, then
+//           (lo.z, hi.z) of both (pairs of the packed slab FMAs),
 //           then (ref0, ref1, order, 0). ref >= 0 is an inner node, ref < 0
 //           is the leaf ~k whose triangle is tpre[k]; bit o of `order` set:
 //           child 1 is visited first by rays of sign octant o.

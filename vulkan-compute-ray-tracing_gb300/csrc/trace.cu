@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
         const float4 *N = bvh + 4ll * node;
         float4 a, b, c, d;
         load_node(N, a, b, c, d);
-        const bool h0 = slab_hit(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-        const bool h1 = slab_hit(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+        const bool h0 = slab_hit_child0(r, a, c, closest);
+        const bool h1 = slab_hit_child1(r, b, c, closest);
         int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
         if (h0 && h1) {
           const bool f1 = child1_first(d, ray_octant(r));
@@ -495,7 +495,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
             ray_s[lane][1] = r1;
             key_v[lane] = (unsigned long long)ord_f(__fadd_rn(r1.w, 0.0f)) << 32;
             r = make_ray(mk3(r0.x, r0.y, r0.z), mk3(r1.x, r1.y, r1.z), r0.w);
-            oct = (r.ix < 0.0f ? 1u : 0u) | (r.iy < 0.0f ? 2u : 0u) | (r.iz < 0.0f ? 4u : 0u);
+            oct = (uint32_t)ray_octant(r);
             ray_i = (int)i;
             gsp = 0;
             gmask = 0;
@@ -541,10 +541,10 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
           load_slot8(N + 2, q2, q3);
           load_slot8(N + 4, q4, q5);
           const uint32_t ew = __float_as_uint(q0.w);
-            const float sx = r.ix * pow2i((int)(int8_t)(ew & 0xffu));
-          const float sy = r.iy * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
-          const float sz = r.iz * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
-          const float ax = (q0.x - r.o.x) * r.ix, ay = (q0.y - r.o.y) * r.iy, az = (q0.z - r.o.z) * r.iz;
+          const float sx = r.ix() * pow2i((int)(int8_t)(ew & 0xffu));
+          const float sy = r.iy() * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
+          const float sz = r.iz() * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
+          const float ax = (q0.x - r.o.x) * r.ix(), ay = (q0.y - r.o.y) * r.iy(), az = (q0.z - r.o.z) * r.iz();
           // Near and far byte words per axis (slots 0-3, 4-7): lo for a
           // positive 1/d, hi for a negative one.
           const bool fx = (oct & 1u) != 0, fy = (oct & 2u) != 0, fz = (oct & 4u) != 0;

@@ -17,11 +17,17 @@
 
 namespace rtgb {
 
+// The slab planes of a box are entered at fma(plane, 1/d, -o/d), computed
+// two at a time with packed FMAs: (lo.x, lo.y) and (hi.x, hi.y) against
+// (1/dx, 1/dy), (lo.z, hi.z) against (1/dz, 1/dz).
 struct TraceRay {
   f3 o, d;
-  float ix, iy, iz;     // 1 / d (tiny components clamped)
-  float ox, oy, oz;     // o / d, for fma slab planes
+  f2 ixy, izz;  // 1 / d (tiny components clamped) as (x, y) and (z, z)
+  f2 nxy, nzz;  // -o / d in the same pairs
   float tmin;
+  __device__ __forceinline__ float ix() const { return lo2(ixy); }
+  __device__ __forceinline__ float iy() const { return hi2(ixy); }
+  __device__ __forceinline__ float iz() const { return lo2(izz); }
 };
 
 __device__ __forceinline__ float safe_rcp(float x) {
@@ -33,12 +39,12 @@ __device__ __forceinline__ TraceRay make_ray(f3 o, f3 d, float tmin) {
   TraceRay r;
   r.o = o;
   r.d = d;
-  r.ix = safe_rcp(d.x);
-  r.iy = safe_rcp(d.y);
-  r.iz = safe_rcp(d.z);
-  r.ox = o.x * r.ix;
-  r.oy = o.y * r.iy;
-  r.oz = o.z * r.iz;
+  const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
+  const float ox = __fmul_rn(o.x, ix), oy = __fmul_rn(o.y, iy), oz = __fmul_rn(o.z, iz);
+  r.ixy = pk2(ix, iy);
+  r.izz = pk2(iz, iz);
+  r.nxy = pk2(-ox, -oy);
+  r.nzz = pk2(-oz, -oz);
   r.tmin = tmin;
   return r;
 }
@@ -79,12 +85,12 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // lo <= hi both forms give the same bits: fma(lo, i, -o) <= fma(hi, i, -o)
 // for i > 0 because rounding is monotonic, so min/max pick exactly those
 // values. The fixed form saves six ALU operations per box.
+// The box is given as the pairs (lo.x, lo.y), (hi.x, hi.y), (lo.z, hi.z).
 template <int OCT = -1>
-__device__ __forceinline__ void slab_span(const TraceRay &r, float lx, float hx, float ly, float hy, float lz, float hz,
-                                          float tmax, float &tn, float &tf) {
-  float ax = fmaf(lx, r.ix, -r.ox), bx = fmaf(hx, r.ix, -r.ox);
-  float ay = fmaf(ly, r.iy, -r.oy), by = fmaf(hy, r.iy, -r.oy);
-  float az = fmaf(lz, r.iz, -r.oz), bz = fmaf(hz, r.iz, -r.oz);
+__device__ __forceinline__ void slab_span(const TraceRay &r, f2 lxy, f2 hxy, f2 lhz, float tmax, float &tn,
+                                          float &tf) {
+  const f2 pa = fma2(lxy, r.ixy, r.nxy), pb = fma2(hxy, r.ixy, r.nxy), pz = fma2(lhz, r.izz, r.nzz);
+  const float ax = lo2(pa), ay = hi2(pa), bx = lo2(pb), by = hi2(pb), az = lo2(pz), bz = hi2(pz);
   if (OCT < 0) {
     tn = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), r.tmin));
     tf = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
@@ -101,16 +107,22 @@ template <int OCT = -1>
 __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float hx, float ly, float hy, float lz,
                                             float hz, float tmax) {
   float tn, tf;
-  slab_span<OCT>(r, lx, hx, ly, hy, lz, hz, tmax, tn, tf);
+  slab_span<OCT>(r, pk2(lx, ly), pk2(hx, hy), pk2(lz, hz), tmax, tn, tf);
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
 
-// The same test as a flag, for loops that order children without distances.
+// The same test as a flag, for loops that order children without distances,
+// on child 0 or 1 of a pair node loaded as (a, b, c, d) (load_node).
 template <int OCT = -1>
-__device__ __forceinline__ bool slab_hit(const TraceRay &r, float lx, float hx, float ly, float hy, float lz, float hz,
-                                         float tmax) {
+__device__ __forceinline__ bool slab_hit_child0(const TraceRay &r, float4 a, float4 c, float tmax) {
   float tn, tf;
-  slab_span<OCT>(r, lx, hx, ly, hy, lz, hz, tmax, tn, tf);
+  slab_span<OCT>(r, pk2(a.x, a.y), pk2(a.z, a.w), pk2(c.x, c.y), tmax, tn, tf);
+  return tn <= tf;
+}
+template <int OCT = -1>
+__device__ __forceinline__ bool slab_hit_child1(const TraceRay &r, float4 b, float4 c, float tmax) {
+  float tn, tf;
+  slab_span<OCT>(r, pk2(b.x, b.y), pk2(b.z, b.w), pk2(c.z, c.w), tmax, tn, tf);
   return tn <= tf;
 }
 
@@ -121,7 +133,7 @@ __device__ __forceinline__ bool child1_first(float4 d, int oct) { return (__floa
 
 // Sign octant of the ray's inverse direction (the OCT of slab_enter).
 __device__ __forceinline__ int ray_octant(const TraceRay &r) {
-  return (r.ix < 0.0f ? 1 : 0) | (r.iy < 0.0f ? 2 : 0) | (r.iz < 0.0f ? 4 : 0);
+  return (r.ix() < 0.0f ? 1 : 0) | (r.iy() < 0.0f ? 2 : 0) | (r.iz() < 0.0f ? 4 : 0);
 }
 
 // The octant shared by every active lane of the warp, or -1 (mixed, or no
@@ -186,8 +198,8 @@ __device__ __forceinline__ int traverse_closest_on(const DevScene &sc, const Tra
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      const bool h0 = slab_hit(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      const bool h1 = slab_hit(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      const bool h0 = slab_hit_child0(r, a, c, closest);
+      const bool h1 = slab_hit_child1(r, b, c, closest);
       int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
       if (h0 && h1) {
         const bool f1 = child1_first(d, oct);
@@ -256,8 +268,8 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      const bool h0 = slab_hit<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest);
-      const bool h1 = slab_hit<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest);
+      const bool h0 = slab_hit_child0<OCT>(r, a, c, closest);
+      const bool h1 = slab_hit_child1<OCT>(r, b, c, closest);
       int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
       if (h0 && h1) {
         const bool f1 = child1_first(d, oct);
@@ -350,8 +362,8 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      const bool any0 = __any_sync(0xffffffffu, slab_hit<OCT>(r, a.x, a.y, a.z, a.w, c.x, c.y, closest));
-      const bool any1 = __any_sync(0xffffffffu, slab_hit<OCT>(r, b.x, b.y, b.z, b.w, c.z, c.w, closest));
+      const bool any0 = __any_sync(0xffffffffu, slab_hit_child0<OCT>(r, a, c, closest));
+      const bool any1 = __any_sync(0xffffffffu, slab_hit_child1<OCT>(r, b, c, closest));
       const int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
       if (any0 && any1) {
         const bool f1 = child1_first(d, oct);
