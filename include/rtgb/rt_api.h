@@ -289,8 +289,7 @@ rt_status rtReadSegmentCounter(rt_ctx *ctx, uint64_t *out, int reset);
  * Returns once the nodes are written, and on every error path only after the
  * work it queued has finished. The first call on each device, with that
  * device current, looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture
- * begins. Calls share the array, which keeps the last call's contents: they
+ * (cudaGetSymbolAddress). Calls share the array, which keeps the last call's contents: they
  * are serialised inside the library, and GPU work that overlaps a call on
  * the same device from outside the library and touches the array races.
  * Both pointers must be 16-byte aligned. */
