@@ -826,8 +826,9 @@ void oracle_denoise(const float *in, uint32_t W, uint32_t H, float sigma, float 
 // quantizes each node with the library's host quantizer (96-byte words) and
 // oracle_trace_wide traverses those words: planes entered at fmaf(q, ix *
 // 2^e, (o - ray.o) * ix), the entered inner child of smallest entry distance
-// visited next and the others later in increasing order of slot ^ (the
-// ray's direction sign bits), triangles tested when reached
+// (compared with the slot in the distance's low three bits) visited next and
+// the others later in increasing order of slot ^ (the ray's direction sign
+// bits), triangles tested when reached
 // with the acceptance rule of the culled traversal (exactly equal t: the
 // lower triangle index wins).
 
@@ -1038,8 +1039,11 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
         sc[k] = inv[k] * p2;
         ax[k] = (org[k] - r.o[k]) * inv[k];
       }
-      uint32_t ibits = 0, nearest = 0;
-      float tbest = INFINITY;
+      // The nearest entered inner child: the minimum of keys (entry distance
+      // with its low three bits replaced by the slot), the lowest such slot
+      // when no key is finite.
+      uint32_t hin = 0;
+      float kbest = INFINITY;
       for (int s = 0; s < 8; s++) {
         if (!((fmask >> s) & 1u)) continue;
         const int32_t ref = (int32_t)w[16 + s];
@@ -1056,11 +1060,13 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
                                    std::fmin(std::fmax(t[2], t[5]), closest));
         if (!(n0 <= f0)) continue;
         if (ref >= 0) {
-          ibits |= 1u << ((uint32_t)s ^ oct);
-          if (n0 < tbest) {
-            tbest = n0;
-            nearest = (uint32_t)s;
-          }
+          hin |= 1u << s;
+          uint32_t kb;
+          std::memcpy(&kb, &n0, 4);
+          kb = (kb & ~7u) | (uint32_t)s;
+          float key;
+          std::memcpy(&key, &kb, 4);
+          kbest = std::fmin(kbest, key);
           continue;
         }
         const int32_t tri = ~ref;
@@ -1081,7 +1087,16 @@ int oracle_trace_wide(const rt_triangle *tris, uint32_t ntris, const uint32_t *q
         }
       }
       node = -1;
-      if (ibits) {
+      if (hin) {
+        uint32_t nearest = (uint32_t)__builtin_ctz(hin);
+        if (kbest < INFINITY) {
+          uint32_t kb;
+          std::memcpy(&kb, &kbest, 4);
+          nearest = kb & 7u;
+        }
+        uint32_t ibits = 0;
+        for (int s = 0; s < 8; s++)
+          if ((hin >> s) & 1u) ibits |= 1u << ((uint32_t)s ^ oct);
         // The nearest entered child next, the others later in rank order.
         node = (int32_t)w[16 + nearest];
         const uint32_t rest = ibits & ~(1u << (nearest ^ oct));
