@@ -234,6 +234,11 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   the reference's tree, but closest hits are identical
  *                   (equal-t ties go to the lower triangle index in every
  *                   tree); rtDownloadBvh returns the tree that was built
+ *   "bvh8.collapse"  how rtUploadScene folds the tree into the 8-wide
+ *                   nodes the incoherent caster walks: 1 (default) the
+ *                   folded pairs chosen by the surface area heuristic
+ *                   (least summed node area: fewer node visits), 0 the
+ *                   largest child opened first; the hits are the same
  *   "bvh.test_error_level"  test hook (default -1, off): builder 0 records
  *                   an error bit in its device error word after the sort of
  *                   this tree level, as a sort overflow would, so the upload

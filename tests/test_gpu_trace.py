@@ -409,3 +409,32 @@ def test_block_size_and_stack_depth_keep_hits(rt, ctx, level, wide_min):
         for k, v in zip(keys, old):
             ctx.set_tuning(k, v)
         sc.release()
+
+
+@pytest.mark.parametrize("collapse", [0, 1], ids=["largest-first", "sah"])
+def test_bvh8_collapse_modes_keep_hits(rt, orc, ctx, collapse):
+    """Both 8-wide folds ("bvh8.collapse": SAH-chosen pairs, largest child
+    first) give the oracle's hits bit for bit on the 8-wide caster, for
+    camera and random rays, on a displaced icosphere and on a Cornell soup
+    (long thin triangles, many overlapping boxes)."""
+    keys = ("bvh8.collapse", "trace.wide_min_tris")
+    old = [ctx.get_tuning(k) for k in keys]
+    ctx.set_tuning("bvh8.collapse", collapse)
+    ctx.set_tuning("trace.wide_min_tris", 0)
+    scs = []
+    try:
+        t_ico = rt.gen_icosphere(9, 6)
+        t_box, m_box, _ = rt.gen_cornell(4, 30000, 0)
+        for tris, mats, eye in ((t_ico, rt.gen_cornell(1, 0)[1], [0, 0, -3]), (t_box, m_box, [0, 0, -14])):
+            sc = ctx.upload_scene(tris, mats)
+            scs.append(sc)
+            cam = rt.camera_look_at(eye, [0, 0, 0], [0, 1, 0], 40.0, 96, 64)
+            rays = np.concatenate([rt.gen_camera_rays(cam, 96, 64), rt.gen_random_rays(13, 20000)])
+            want = orc.trace(tris, sc.bvh(), rays)
+            got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    finally:
+        for k, v in zip(keys, old):
+            ctx.set_tuning(k, v)
+        for sc in scs:
+            sc.release()

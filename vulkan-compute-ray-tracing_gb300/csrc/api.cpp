@@ -471,8 +471,13 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   }
   // The 8-wide fold of the same tree.
   {
+    bool sah = true;
+    {
+      std::lock_guard<std::mutex> g(ctx->mu);
+      sah = ctx->build_opts.collapse != 0;
+    }
     char errbuf[128] = {0};
-    cudaError_t be = build_bvh8(d, slab + off_bvh8, bvh8_capacity(nt), &d.n8, &d.levels8, &d.root8, errbuf,
+    cudaError_t be = build_bvh8(d, sah, slab + off_bvh8, bvh8_capacity(nt), &d.n8, &d.levels8, &d.root8, errbuf,
                                 sizeof(errbuf), st);
     if (be != cudaSuccess && errbuf[0]) return abort_upload(fail(ctx, RT_ERR_INTERNAL, "%s", errbuf));
     UCK(be, "bvh8");
@@ -821,6 +826,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->build_opts.builder = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "bvh8.collapse") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->build_opts.collapse = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "bvh.test_error_level") {
     if (value < -1 || value > 64) return RT_ERR_INVALID_ARGUMENT;
     ctx->build_opts.test_error_level = (int)value;
@@ -912,6 +922,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "bvh.builder") {
     *value = ctx->build_opts.builder;
+    return RT_SUCCESS;
+  }
+  if (k == "bvh8.collapse") {
+    *value = ctx->build_opts.collapse;
     return RT_SUCCESS;
   }
   if (k == "bvh.test_error_level") {

@@ -177,11 +177,149 @@ __device__ __forceinline__ void load_pair(const float4 *__restrict__ bvh2, int32
   c1.ref = __float_as_int(d.y);
 }
 
+// ---- SAH collapse: which bvh2 pairs become 8-wide nodes.
+// A ray reaches an 8-wide node with probability proportional to the node's
+// box area, and every leaf occupies one slot wherever it goes, so the fold
+// that minimises the summed area of the chosen nodes minimises the expected
+// node visits (the surface area heuristic with fixed leaf cost). Bottom-up
+// over the pairs: D(p, j), j = 1..8, is the least summed area for covering
+// pair p's subtree with at most j slots, either p itself as one slot (it
+// becomes a node: C(p) = area(p) + the best split of 8 slots between its
+// children) or its children splitting the j slots; a leaf costs 0. Each
+// pair stores D(p, 1..8) and its choices: the split of j slots for j = 2..8
+// (0: p stays one slot) and the split of 8 slots when p is a node.
+
+// Parent pair of every inner pair and of every leaf (the root pair: -1).
+__global__ void k_pair_parents(const float4 *__restrict__ bvh2, uint32_t n_pairs, int32_t *__restrict__ parent,
+                               int32_t *__restrict__ leaf_parent, uint32_t ntris, uint32_t *__restrict__ err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const float4 d = bvh2[4ull * p + 3];
+  const int32_t refs[2] = {__float_as_int(d.x), __float_as_int(d.y)};
+  for (int c = 0; c < 2; c++) {
+    const int32_t r = refs[c];
+    if (r >= 0 ? (uint32_t)r >= n_pairs : (uint32_t)~r >= ntris) {
+      atomicOr(err, 1u);
+      continue;
+    }
+    if (r >= 0) parent[r] = (int32_t)p;
+    else leaf_parent[~r] = (int32_t)p;
+  }
+}
+
+// One thread per leaf climbs towards the root; the second thread to reach a
+// pair (both children done) computes its costs and climbs on.
+__global__ void k_collapse_costs(const float4 *__restrict__ bvh2, uint32_t n_pairs, uint32_t ntris,
+                                 const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
+                                 uint32_t *__restrict__ arrivals, float *__restrict__ cost,
+                                 uint32_t *__restrict__ choice, uint32_t *__restrict__ err) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ntris) return;
+  int32_t p = leaf_parent[k];
+  for (int climb = 0; p >= 0; climb++) {
+    if ((uint32_t)p >= n_pairs || climb > 128) {
+      atomicOr(err, 1u);
+      return;
+    }
+    if (atomicAdd(arrivals + p, 1u) == 0u) return;
+    __threadfence();
+    Slot c[2];
+    load_pair(bvh2, p, c[0], c[1]);
+    if ((c[0].ref >= 0 && (uint32_t)c[0].ref >= n_pairs) || (c[1].ref >= 0 && (uint32_t)c[1].ref >= n_pairs)) {
+      atomicOr(err, 1u);
+      return;
+    }
+    float dc[2][9];
+    for (int i = 0; i < 2; i++)
+      for (int j = 1; j <= 8; j++) dc[i][j] = c[i].ref >= 0 ? __ldcg(cost + 8ull * c[i].ref + (j - 1)) : 0.0f;
+    Slot u = c[0];
+    for (int a = 0; a < 3; a++) {
+      u.lo[a] = fminf(c[0].lo[a], c[1].lo[a]);
+      u.hi[a] = fmaxf(c[0].hi[a], c[1].hi[a]);
+    }
+    // Best split of j slots between the children, the lower left share first on ties.
+    auto split = [&](int j, int &kbest) {
+      float best = __int_as_float(0x7f800000);
+      kbest = 1;
+      for (int l = 1; l < j; l++) {
+        const float v = dc[0][l] + dc[1][j - l];
+        if (v < best) {
+          best = v;
+          kbest = l;
+        }
+      }
+      return best;
+    };
+    int k8;
+    const float as_node = slot_area(u) + split(8, k8);
+    uint32_t ch = (uint32_t)k8 << 28;
+    __stcg(cost + 8ull * p, as_node);
+    for (int j = 2; j <= 8; j++) {
+      int kj;
+      const float v = split(j, kj);
+      const bool keep = as_node <= v;
+      __stcg(cost + 8ull * p + (j - 1), keep ? as_node : v);
+      if (!keep) ch |= (uint32_t)kj << (4 * (j - 2));
+    }
+    __stcg(choice + p, ch);
+    __threadfence();
+    p = parent[p];
+  }
+}
+
+// The SAH choices expanded: pair p0's slots as a node.
+__device__ __forceinline__ int sah_slots(const float4 *__restrict__ bvh2, uint32_t n_pairs,
+                                         const uint32_t *__restrict__ choice, int32_t p0, Slot (&S)[8],
+                                         uint32_t *__restrict__ err) {
+  struct Item {
+    Slot s;
+    int j;
+  };
+  Item st[8];
+  int sp = 0, cnt = 0;
+  Slot c0, c1;
+  load_pair(bvh2, p0, c0, c1);
+  const int k8 = (int)(__ldg(choice + p0) >> 28);
+  if (k8 < 1 || k8 > 7) {
+    atomicOr(err, 1u);
+    return 0;
+  }
+  st[sp++] = Item{c1, 8 - k8};
+  st[sp++] = Item{c0, k8};
+  while (sp > 0) {
+    const Item it = st[--sp];
+    int kj = 0;
+    if (it.s.ref >= 0 && it.j >= 2) {
+      if ((uint32_t)it.s.ref >= n_pairs) {
+        atomicOr(err, 1u);
+        return 0;
+      }
+      kj = (int)((__ldg(choice + it.s.ref) >> (4 * (it.j - 2))) & 15u);
+    }
+    if (kj == 0) {
+      if (cnt >= 8) {
+        atomicOr(err, 1u);
+        return 0;
+      }
+      S[cnt++] = it.s;
+      continue;
+    }
+    if (kj >= it.j || sp + 2 > 8) {
+      atomicOr(err, 1u);
+      return 0;
+    }
+    load_pair(bvh2, it.s.ref, c0, c1);
+    st[sp++] = Item{c1, it.j - kj};
+    st[sp++] = Item{c0, kj};
+  }
+  return cnt;
+}
+
 // One frontier node per thread: bvh2 pair frontier[f] becomes bvh8 node
 // base + f. inner_cnt[f] receives its number of inner children.
 __global__ void k_collapse8(const float4 *__restrict__ bvh2, uint32_t n_pairs, const int32_t *__restrict__ frontier,
                             uint32_t count, uint32_t base, float4 *__restrict__ bvh8, uint32_t *__restrict__ inner_cnt,
-                            uint32_t *__restrict__ err) {
+                            const uint32_t *__restrict__ choice, uint32_t *__restrict__ err) {
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= count) return;
   Slot S[8];
@@ -189,6 +327,8 @@ __global__ void k_collapse8(const float4 *__restrict__ bvh2, uint32_t n_pairs, c
   const int32_t p0 = frontier[f];
   if (p0 < 0 || (uint32_t)p0 >= n_pairs) {
     atomicOr(err, 1u);
+  } else if (choice) {
+    cnt = sah_slots(bvh2, n_pairs, choice, p0, S, err);
   } else {
     load_pair(bvh2, p0, S[0], S[1]);
     cnt = 2;
@@ -305,9 +445,26 @@ uint32_t bvh8_capacity(uint32_t ntris) { return ntris ? (uint32_t)((4ull * ntris
 
 namespace {
 
-// The fp32 fold (256-byte nodes) into `bvh8`, which holds `cap` nodes.
-cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
-                            int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
+// The SAH choices of every pair (k_collapse_costs) into `choice`; `scr`
+// holds 10 words per pair plus one per leaf.
+cudaError_t collapse_choices(const DevScene &d, uint32_t *scr, uint32_t *choice, uint32_t *errw, cudaStream_t st) {
+  const uint32_t n_pairs = d.ntris - 1;
+  int32_t *parent = (int32_t *)scr, *leaf_parent = (int32_t *)(scr + n_pairs);
+  uint32_t *arrivals = scr + n_pairs + d.ntris;
+  float *cost = (float *)(arrivals + n_pairs);
+  cudaError_t e = cudaMemsetAsync(parent, 0xff, 4ull * (n_pairs + d.ntris), st);  // parent, leaf_parent: -1
+  if (e == cudaSuccess) e = cudaMemsetAsync(arrivals, 0, 4ull * n_pairs, st);
+  if (e != cudaSuccess) return e;
+  k_pair_parents<<<(n_pairs + 255) / 256, 256, 0, st>>>(d.bvh2, n_pairs, parent, leaf_parent, d.ntris, errw);
+  k_collapse_costs<<<(d.ntris + 255) / 256, 256, 0, st>>>(d.bvh2, n_pairs, d.ntris, parent, leaf_parent, arrivals,
+                                                          cost, choice, errw);
+  return cudaGetLastError();
+}
+
+// The fp32 fold (256-byte nodes) into `bvh8`, which holds `cap` nodes:
+// pairs chosen by the SAH (sah) or by opening the largest child first.
+cudaError_t build_wide_fp32(const DevScene &d, bool sah, float4 *bvh8, uint32_t cap, uint32_t *n8_out,
+                            uint32_t *levels_out, int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
   *n8_out = 0;
   *levels_out = 0;
   *root_out = 0;  // node 0
@@ -337,15 +494,20 @@ cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint3
   }
   const uint32_t n_pairs = d.ntris - 1;
   // Scratch: two frontiers, counts, offsets (cap words each), scan sums, error word.
-  const size_t words = 4ull * cap + cap / 1024 + 8;
+  // With the SAH: the pairs' choices, and for their computation the parent
+  // links, arrival counters and costs (11 words per pair, 1 per leaf).
+  const size_t sah_words = sah ? 11ull * n_pairs + d.ntris : 0;
+  const size_t words = 4ull * cap + cap / 1024 + 8 + sah_words;
   uint32_t *scr = nullptr;
   cudaError_t e = cudaMallocAsync((void **)&scr, 4 * words, st);
   if (e != cudaSuccess) return e;
   int32_t *fr = (int32_t *)scr, *fr_next = (int32_t *)(scr + cap);
   uint32_t *cnt = scr + 2ull * cap, *offs = scr + 3ull * cap, *errw = scr + 4ull * cap;
   uint32_t *sums = errw + 4;
+  uint32_t *choice = sah ? sums + cap / 1024 + 4 : nullptr;
   e = cudaMemsetAsync(errw, 0, 4, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(fr, 0, 4, st);  // the root pair is bvh2 record 0
+  if (e == cudaSuccess && sah) e = collapse_choices(d, choice + n_pairs, choice, errw, st);
   uint32_t count = 1, base = 0, levels = 0, bad = 0;
   while (e == cudaSuccess && count > 0) {
     if (base + count > cap) {
@@ -353,7 +515,7 @@ cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint3
       break;
     }
     const uint32_t grid = (count + 255) / 256;
-    k_collapse8<<<grid, 256, 0, st>>>(d.bvh2, n_pairs, fr, count, base, bvh8, cnt, errw);
+    k_collapse8<<<grid, 256, 0, st>>>(d.bvh2, n_pairs, fr, count, base, bvh8, cnt, choice, errw);
     e = exclusive_scan_u32(cnt, offs, sums, count, st);
     if (e != cudaSuccess) break;
     k_link8<<<grid, 256, 0, st>>>(count, base, base + count, offs, bvh8, fr_next, cap, errw);
@@ -398,8 +560,8 @@ cudaError_t build_wide_fp32(const DevScene &d, float4 *bvh8, uint32_t cap, uint3
 
 }  // namespace
 
-cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
-                       int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
+cudaError_t build_bvh8(const DevScene &d, bool sah, void *bvh8q, uint32_t cap, uint32_t *n8_out,
+                       uint32_t *levels_out, int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st) {
   *n8_out = 0;
   *levels_out = 0;
   if (d.ntris == 0 || cap == 0 || !bvh8q) return cudaErrorInvalidValue;
@@ -408,7 +570,13 @@ cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n
   if (e != cudaSuccess) return e;
   uint32_t *errw = reinterpret_cast<uint32_t *>(wide + 16ull * cap);
   uint32_t n8 = 0, levels = 0;
-  e = build_wide_fp32(d, wide, cap, &n8, &levels, root_out, errbuf, errlen, st);
+  e = build_wide_fp32(d, sah, wide, cap, &n8, &levels, root_out, errbuf, errlen, st);
+  // The SAH fold has no node bound below one per pair: past the capacity
+  // sized for the largest-first fold, take that fold instead.
+  if (e == cudaErrorInvalidValue && sah && strstr(errbuf, "capacity")) {
+    errbuf[0] = 0;
+    e = build_wide_fp32(d, false, wide, cap, &n8, &levels, root_out, errbuf, errlen, st);
+  }
   uint32_t bad = 0;
   if (e == cudaSuccess) e = cudaMemsetAsync(errw, 0, 4, st);
   if (e == cudaSuccess) {

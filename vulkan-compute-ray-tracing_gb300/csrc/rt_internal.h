@@ -64,10 +64,11 @@ struct DevScene {
 // Node capacity the collapse may need for `ntris` leaves: (4n - 1) / 7 + 1.
 uint32_t bvh8_capacity(uint32_t ntris);
 // Folds d.bvh2 into quantized bvh8 nodes (96 B each, capacity `cap`
-// nodes); synchronises `st`.
+// nodes), choosing the folded pairs by the SAH (`sah`) or largest child
+// first; synchronises `st`.
 constexpr size_t kBvh8NodeBytes = 96;
-cudaError_t build_bvh8(const DevScene &d, void *bvh8q, uint32_t cap, uint32_t *n8_out, uint32_t *levels_out,
-                       int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st);
+cudaError_t build_bvh8(const DevScene &d, bool sah, void *bvh8q, uint32_t cap, uint32_t *n8_out,
+                       uint32_t *levels_out, int32_t *root_out, char *errbuf, size_t errlen, cudaStream_t st);
 
 // ---------------------------------------------------------------- relayout.cu
 // Exclusive scan of n words (in may equal out); `sums` needs ceil(n/1024).
@@ -180,6 +181,7 @@ inline bool use_wavefront_batched(const RenderOpts &o, const rt_render_params &p
 // Tree used when a scene is uploaded without nodes (rtSetTuning "bvh.builder").
 struct BuildOpts {
   int builder = 0;  // 0 the reference's Bvh.h tree (bit-exact), 1 LBVH, 2 PLOC
+  int collapse = 1;  // 8-wide fold: 1 SAH-chosen pairs, 0 largest child first ("bvh8.collapse")
   int test_error_level = -1;  // test hook of gpu_build_bvh's error word (-1: off)
 };
 
