@@ -45,6 +45,8 @@ def _load():
         "oracle_render_f64": (I32, [P, U32, P, U32, P, U32, P, U32, P, U32, P, P, P, ctypes.POINTER(ctypes.c_uint64), I32]),
         "oracle_max_threads": (I32, []),
         "oracle_wide_fold": (I32, [P, U32, U32, P, P, P, ctypes.POINTER(U32), ctypes.POINTER(U32)]),
+        "oracle_wide_fold_mode": (I32, [P, U32, U32, ctypes.c_int, P, P, P, ctypes.POINTER(U32),
+                                        ctypes.POINTER(U32)]),
         "oracle_octant_slot_assignment": (I32, [P, U32, P]),
         "oracle_trace_wide": (I32, [P, U32, P, U32, I32, P, P, U32, P, P, I32]),
         "oracle_gen_icosphere": (U32, [ctypes.c_uint64, U32, ctypes.c_float, ctypes.c_float, U32, P]),
@@ -294,20 +296,22 @@ def trace(tris, nodes, rays, mode: int = 0, stack_size: int = 16, slack: float =
     return (hits, st) if stats else hits
 
 
-def wide_fold(nodes):
+def wide_fold(nodes, sah: bool = False):
     """The GPU builder's 8-wide fold of a reference node array, restated:
     per node 8 child slots placed by octant (boxes lo.xyz, hi.xyz; refs: the
     child node's number for inner children, ~triangle for leaves, INT_MIN
-    empty) and the mask of filled slots. Returns (boxes (n8, 8, 6), refs
-    (n8, 8), fmask (n8,), levels)."""
+    empty) and the mask of filled slots; the folded nodes opened largest
+    child first, or (sah) chosen by the surface area heuristic. Returns
+    (boxes (n8, 8, 6), refs (n8, 8), fmask (n8,), levels)."""
     nodes = np.ascontiguousarray(nodes, np.float32)
-    cap = max(1, (4 * ((len(nodes) + 1) // 2) + 6) // 7 + 1)
+    ntris = (len(nodes) + 1) // 2
+    cap = max(1, ntris if sah else (4 * ntris + 6) // 7 + 1)
     boxes = np.zeros((cap, 8, 6), np.float32)
     refs = np.zeros((cap, 8), np.int32)
     fmask = np.zeros(cap, np.uint32)
     n8, levels = ctypes.c_uint32(0), ctypes.c_uint32(0)
-    rc = LIB.oracle_wide_fold(_p(nodes), len(nodes), cap, _p(boxes), _p(refs), _p(fmask), ctypes.byref(n8),
-                              ctypes.byref(levels))
+    rc = LIB.oracle_wide_fold_mode(_p(nodes), len(nodes), cap, 1 if sah else 0, _p(boxes), _p(refs), _p(fmask),
+                                   ctypes.byref(n8), ctypes.byref(levels))
     if rc != 0:
         raise RuntimeError(f"oracle_wide_fold failed ({rc})")
     n = n8.value

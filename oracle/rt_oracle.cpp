@@ -884,9 +884,25 @@ int oracle_octant_slot_assignment(const float *boxes, uint32_t cnt, int32_t *slo
   return 0;
 }
 
+// mode 1 (the GPU's default "bvh8.collapse"): the inner nodes that become
+// 8-wide nodes are chosen by the surface area heuristic with a fixed leaf
+// cost, least summed node area. D(n, j), j = 1..8, is the least summed area
+// covering n's subtree with at most j slots: n as one slot (n becomes a
+// node: area(n) + the best split of 8 slots between its children) or its
+// children splitting the j slots (left share l = 1..j-1, the lowest of
+// equal sums); a leaf costs 0; n stays one slot when that is not dearer.
+// The area of an inner node is that of its children's box union.
+int oracle_wide_fold_mode(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, int mode, float *boxes,
+                          int32_t *refs, uint32_t *fmask_out, uint32_t *n8_out, uint32_t *levels_out);
+
 int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, float *boxes, int32_t *refs,
                      uint32_t *fmask_out, uint32_t *n8_out, uint32_t *levels_out) {
-  if (!nodes || nnodes == 0 || !boxes || !refs || !fmask_out || !n8_out) return 1;
+  return oracle_wide_fold_mode(nodes, nnodes, cap, 0, boxes, refs, fmask_out, n8_out, levels_out);
+}
+
+int oracle_wide_fold_mode(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, int mode, float *boxes,
+                          int32_t *refs, uint32_t *fmask_out, uint32_t *n8_out, uint32_t *levels_out) {
+  if (!nodes || nnodes == 0 || !boxes || !refs || !fmask_out || !n8_out || mode < 0 || mode > 1) return 1;
   struct Slot {
     float b[6];
     int32_t node;  // reference node index
@@ -920,6 +936,67 @@ int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, fl
     for (size_t i = 0; i < S.size(); i++) out[so[i]] = S[i];
     return out;
   };
+  // SAH costs, children before parents (Bvh.h numbers a child after its parent).
+  std::vector<std::array<float, 9>> D;
+  std::vector<std::array<int8_t, 9>> pick_j;  // j = 2..8: left share, 0 = one slot
+  std::vector<int8_t> pick8;                  // split of 8 slots when a node
+  if (mode == 1) {
+    D.assign(nnodes, {});
+    pick_j.assign(nnodes, {});
+    pick8.assign(nnodes, 1);
+    for (int64_t n = (int64_t)nnodes - 1; n >= 0; n--) {
+      if (!inner((int32_t)n)) continue;
+      const int32_t c[2] = {nodes[n].left, nodes[n].right};
+      float dc[2][9];
+      for (int i = 0; i < 2; i++)
+        for (int j = 1; j <= 8; j++) dc[i][j] = inner(c[i]) ? D[c[i]][j] : 0.0f;
+      Slot u = slot_of(c[0]);
+      const Slot v = slot_of(c[1]);
+      for (int k = 0; k < 3; k++) {
+        u.b[k] = std::fmin(u.b[k], v.b[k]);
+        u.b[3 + k] = std::fmax(u.b[3 + k], v.b[3 + k]);
+      }
+      auto split = [&](int j, int &kbest) {
+        float best = INFINITY;
+        kbest = 1;
+        for (int l = 1; l < j; l++) {
+          const float x = dc[0][l] + dc[1][j - l];
+          if (x < best) {
+            best = x;
+            kbest = l;
+          }
+        }
+        return best;
+      };
+      int k8;
+      const float as_node = area(u) + split(8, k8);
+      pick8[n] = (int8_t)k8;
+      D[n][1] = as_node;
+      for (int j = 2; j <= 8; j++) {
+        int kj;
+        const float x = split(j, kj);
+        const bool keep = as_node <= x;
+        D[n][j] = keep ? as_node : x;
+        pick_j[n][j] = keep ? 0 : (int8_t)kj;
+      }
+    }
+  }
+  auto sah_children = [&](int32_t f) {
+    std::vector<Slot> S;
+    std::vector<std::pair<int32_t, int>> st = {{nodes[f].right, 8 - pick8[f]}, {nodes[f].left, pick8[f]}};
+    while (!st.empty()) {
+      const auto [m, j] = st.back();
+      st.pop_back();
+      const int kj = (inner(m) && j >= 2) ? pick_j[m][j] : 0;
+      if (kj == 0) {
+        S.push_back(slot_of(m));
+        continue;
+      }
+      st.push_back({nodes[m].right, j - kj});
+      st.push_back({nodes[m].left, kj});
+    }
+    return S;
+  };
   if (!inner(0)) {
     std::array<Slot, 8> one;
     for (auto &o : one) o.node = -1;
@@ -932,7 +1009,8 @@ int oracle_wide_fold(const rt_bvh_node *nodes, uint32_t nnodes, uint32_t cap, fl
       next.clear();
       for (int32_t f : frontier) {
         std::vector<Slot> S = {slot_of(nodes[f].left), slot_of(nodes[f].right)};
-        while (S.size() < 8) {
+        if (mode == 1) S = sah_children(f);
+        while (mode == 0 && S.size() < 8) {
           int pick = -1;
           float best = -1.0f;
           for (size_t i = 0; i < S.size(); i++) {

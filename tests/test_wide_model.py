@@ -1,7 +1,7 @@
 """The GPU's 8-wide closest-hit traversal checked on the host.
 
-The oracle restates the fold (oracle_wide_fold, the GPU builder's greedy
-rule) and the traversal (oracle_trace_wide: the kernel's fp32 plane
+The oracle restates the fold (oracle_wide_fold: the GPU builder's
+largest-first rule and its SAH-chosen nodes) and the traversal (oracle_trace_wide: the kernel's fp32 plane
 arithmetic on quantized nodes, near-first order, the triangle-index tie
 rule); the nodes are quantized by the library's own host quantizer
 (rtgbQuantizeNode8, the function the upload runs on the GPU). The hits
@@ -24,8 +24,8 @@ def quantize_all(rt, boxes, refs, fmask):
     return words
 
 
-def wide_hits(rt, orc, tris, nodes, rays, stats=False):
-    boxes, refs, fmask, levels = orc.wide_fold(nodes)
+def wide_hits(rt, orc, tris, nodes, rays, stats=False, sah=False):
+    boxes, refs, fmask, levels = orc.wide_fold(nodes, sah)
     assert levels >= 1 and (fmask >= 1).all() and (fmask <= 255).all()
     # Every triangle sits in exactly one leaf slot; empty slots match the mask.
     empty = refs == np.iinfo(np.int32).min
@@ -40,11 +40,28 @@ def wide_hits(rt, orc, tris, nodes, rays, stats=False):
 
 
 def check(rt, orc, tris, rays):
+    """Both folds: largest child first and SAH-chosen nodes."""
     nodes, _ = orc.build_bvh(tris, 1)
     want = orc.trace(tris, nodes, rays)
-    got = wide_hits(rt, orc, tris, nodes, rays)
-    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    for sah in (False, True):
+        got = wide_hits(rt, orc, tris, nodes, rays, sah=sah)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), sah
     assert (want.view(np.int32)[:, 0] >= 0).mean() > 0.2
+
+
+def test_sah_fold_visits_fewer_nodes(rt, orc):
+    """The SAH-chosen fold of the closest-hit mesh family has fewer nodes
+    and costs incoherent rays fewer node visits than largest-first."""
+    tris = rt.gen_icosphere(1, 6)
+    nodes, _ = orc.build_bvh(tris, 1)
+    rays = rt.gen_random_rays(3, 8192)
+    visits = []
+    for sah in (False, True):
+        boxes, _, _, _ = orc.wide_fold(nodes, sah)
+        _, st = wide_hits(rt, orc, tris, nodes, rays, stats=True, sah=sah)
+        visits.append((len(boxes), st[:, 0].mean()))
+    assert visits[1][0] < visits[0][0]
+    assert visits[1][1] < 0.97 * visits[0][1], visits
 
 
 def test_icosphere_camera_and_random(rt, orc):
