@@ -816,18 +816,21 @@ cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t ca
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
   const float4 *r4 = reinterpret_cast<const float4 *>(rays);
-  const size_t smem = (size_t)(kTraceBlock / 32) * wide_warp_smem<1>();
-  auto go = [&](auto kern) {
+  // minblocks 8: one node step per iteration (64 registers); otherwise three.
+  auto go = [&](auto kern, size_t warp_smem) {
+    const size_t smem = (size_t)(kTraceBlock / 32) * warp_smem;
     kern<<<persistent_grid(kern, cap, kTraceBlock, smem), kTraceBlock, smem, st>>>(sc, r4, cap, d_n, hits, counter,
                                                                                    err, perm, list, list_count,
                                                                                    refill, false);
     return cudaGetLastError();
   };
+  const bool narrow = minblocks >= 8;
+  const size_t s1 = wide_warp_smem<1>(), s3 = wide_warp_smem<3>();
   if (sc.levels8 <= 16)
-    return minblocks >= 8 ? go(k_trace_wide<16, 8, true, 1>) : go(k_trace_wide<16, 6, true, 1>);
+    return narrow ? go(k_trace_wide<16, 8, true, 1>, s1) : go(k_trace_wide<16, 6, true, 3>, s3);
   if (sc.levels8 <= 32)
-    return minblocks >= 8 ? go(k_trace_wide<32, 8, true, 1>) : go(k_trace_wide<32, 6, true, 1>);
-  return minblocks >= 8 ? go(k_trace_wide<64, 8, true, 1>) : go(k_trace_wide<64, 6, true, 1>);
+    return narrow ? go(k_trace_wide<32, 8, true, 1>, s1) : go(k_trace_wide<32, 6, true, 3>, s3);
+  return narrow ? go(k_trace_wide<64, 8, true, 1>, s1) : go(k_trace_wide<64, 6, true, 3>, s3);
 }
 
 size_t trace_chunk_scratch_bytes(uint32_t n) { return 4ull * (64 + (n + 31) / 32); }
