@@ -171,10 +171,10 @@ __device__ __forceinline__ float slot_area(const Slot &s) {
 __device__ __forceinline__ void load_pair(const float4 *__restrict__ bvh2, int32_t p, Slot &c0, Slot &c1) {
   const float4 *N = bvh2 + 4ll * p;
   const float4 a = N[0], b = N[1], c = N[2], d = N[3];
-  c0.lo[0] = a.x, c0.lo[1] = a.y, c0.hi[0] = a.z, c0.hi[1] = a.w, c0.lo[2] = c.x, c0.hi[2] = c.y;
-  c1.lo[0] = b.x, c1.lo[1] = b.y, c1.hi[0] = b.z, c1.hi[1] = b.w, c1.lo[2] = c.z, c1.hi[2] = c.w;
-  c0.ref = __float_as_int(d.x);
-  c1.ref = __float_as_int(d.y);
+  c0.lo[0] = a.x, c0.lo[1] = a.y, c0.hi[0] = a.z, c0.hi[1] = a.w, c0.lo[2] = b.x, c0.hi[2] = b.y;
+  c1.lo[0] = c.x, c1.lo[1] = c.y, c1.hi[0] = c.z, c1.hi[1] = c.w, c1.lo[2] = d.x, c1.hi[2] = d.y;
+  c0.ref = __float_as_int(b.z);
+  c1.ref = __float_as_int(d.z);
 }
 
 // ---- SAH collapse: which bvh2 pairs become 8-wide nodes.
@@ -194,8 +194,7 @@ __global__ void k_pair_parents(const float4 *__restrict__ bvh2, uint32_t n_pairs
                                int32_t *__restrict__ leaf_parent, uint32_t ntris, uint32_t *__restrict__ err) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_pairs) return;
-  const float4 d = bvh2[4ull * p + 3];
-  const int32_t refs[2] = {__float_as_int(d.x), __float_as_int(d.y)};
+  const int32_t refs[2] = {__float_as_int(bvh2[4ull * p + 1].z), __float_as_int(bvh2[4ull * p + 3].z)};
   for (int c = 0; c < 2; c++) {
     const int32_t r = refs[c];
     if (r >= 0 ? (uint32_t)r >= n_pairs : (uint32_t)~r >= ntris) {

@@ -129,11 +129,11 @@ __global__ void k_emit(const rt_bvh_node *nodes, uint32_t n, const rt_triangle *
       return cn.left != -1 ? (int32_t)r : ~(int32_t)((uint32_t)c - r);
     };
     float4 *o = bvh2 + 4ull * inner_rank[i];
+    const float order = __uint_as_float(pair_order(c0, c1));
     o[0] = make_float4(c0.min[0], c0.min[1], c0.max[0], c0.max[1]);
-    o[1] = make_float4(c1.min[0], c1.min[1], c1.max[0], c1.max[1]);
-    o[2] = make_float4(c0.min[2], c0.max[2], c1.min[2], c1.max[2]);
-    o[3] = make_float4(__int_as_float(ref(nd.left, c0)), __int_as_float(ref(nd.right, c1)),
-                       __uint_as_float(pair_order(c0, c1)), 0.0f);
+    o[1] = make_float4(c0.min[2], c0.max[2], __int_as_float(ref(nd.left, c0)), order);
+    o[2] = make_float4(c1.min[0], c1.min[1], c1.max[0], c1.max[1]);
+    o[3] = make_float4(c1.min[2], c1.max[2], __int_as_float(ref(nd.right, c1)), order);
   } else {
     uint32_t k = i - inner_rank[i];
     const rt_triangle t = tris[nd.object];

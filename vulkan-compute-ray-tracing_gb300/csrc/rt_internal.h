@@ -22,12 +22,12 @@ enum : uint32_t {
 //   tris    rt_triangle[ntris]   48 B
 //   nodes   rt_bvh_node[nnodes]  48 B, nnodes = 2*ntris - 1
 // Traversal layout (derived on the GPU from `nodes`):
-//   bvh2    4 x float4 per inner node (64 B): the boxes of both children,
-//           (lo.x, lo.y, hi.x, hi.y) of child 0 and of child 1, then
-//           (lo.z, hi.z) of both (pairs of the packed slab FMAs),
-//           then (ref0, ref1, order, 0). ref >= 0 is an inner node, ref < 0
-//           is the leaf ~k whose triangle is tpre[k]; bit o of `order` set:
-//           child 1 is visited first by rays of sign octant o.
+//   bvh2    4 x float4 per inner node (64 B): one 32-byte record per
+//           child, (lo.x, lo.y, hi.x, hi.y) then (lo.z, hi.z, ref, order)
+//           (pairs for the packed slab FMAs). ref >= 0 is an inner node,
+//           ref < 0 is the leaf ~k whose triangle is tpre[k]; bit o of
+//           `order` (the same in both records) set: child 1 is visited
+//           first by rays of sign octant o.
 //   tpre    3 x float4 per triangle in leaf order (48 B): v0, n = cross(b, a),
 //           a = v0 - v1, b = v2 - v0 — the per-triangle terms of triIntersect
 //           (ray-trace-compute.comp:157-173), computed once with the same

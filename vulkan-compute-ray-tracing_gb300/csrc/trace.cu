@@ -121,11 +121,11 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
         const float4 *N = bvh + 4ll * node;
         float4 a, b, c, d;
         load_node(N, a, b, c, d);
-        const bool h0 = slab_hit_child0(r, a, c, closest);
-        const bool h1 = slab_hit_child1(r, b, c, closest);
-        int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+        const bool h0 = slab_hit_child(r, a, b, closest);
+        const bool h1 = slab_hit_child(r, c, d, closest);
+        int r0 = __float_as_int(b.z), r1 = __float_as_int(d.z);
         if (h0 && h1) {
-          const bool f1 = child1_first(d, ray_octant(r));
+          const bool f1 = child1_first(b, ray_octant(r));
           const int nearc = f1 ? r1 : r0, farc = f1 ? r0 : r1;
           if (sp >= STACK) {
             atomicOr(err, KERR_STACK_OVERFLOW);

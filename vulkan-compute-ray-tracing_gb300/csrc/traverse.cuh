@@ -112,24 +112,21 @@ __device__ __forceinline__ float slab_enter(const TraceRay &r, float lx, float h
 }
 
 // The same test as a flag, for loops that order children without distances,
-// on child 0 or 1 of a pair node loaded as (a, b, c, d) (load_node).
+// on one child record of a pair node: (lo.x, lo.y, hi.x, hi.y) in `p`,
+// (lo.z, hi.z, ref, order) in `q` (load_node gives child 0 as (a, b) and
+// child 1 as (c, d)).
 template <int OCT = -1>
-__device__ __forceinline__ bool slab_hit_child0(const TraceRay &r, float4 a, float4 c, float tmax) {
+__device__ __forceinline__ bool slab_hit_child(const TraceRay &r, float4 p, float4 q, float tmax) {
   float tn, tf;
-  slab_span<OCT>(r, pk2(a.x, a.y), pk2(a.z, a.w), pk2(c.x, c.y), tmax, tn, tf);
-  return tn <= tf;
-}
-template <int OCT = -1>
-__device__ __forceinline__ bool slab_hit_child1(const TraceRay &r, float4 b, float4 c, float tmax) {
-  float tn, tf;
-  slab_span<OCT>(r, pk2(b.x, b.y), pk2(b.z, b.w), pk2(c.z, c.w), tmax, tn, tf);
+  slab_span<OCT>(r, pk2(p.x, p.y), pk2(p.z, p.w), pk2(q.x, q.y), tmax, tn, tf);
   return tn <= tf;
 }
 
 // Near-first order at a pair node: true when child 1 is visited first by
-// rays of sign octant `oct` (the node's order bits, relayout.cu). Any order
+// rays of sign octant `oct` (the order bits, in either child record's `q`,
+// relayout.cu). Any order
 // gives the same hit; this one needs no entry distance.
-__device__ __forceinline__ bool child1_first(float4 d, int oct) { return (__float_as_uint(d.z) >> oct) & 1u; }
+__device__ __forceinline__ bool child1_first(float4 q, int oct) { return (__float_as_uint(q.w) >> oct) & 1u; }
 
 // Sign octant of the ray's inverse direction (the OCT of slab_enter).
 __device__ __forceinline__ int ray_octant(const TraceRay &r) {
@@ -198,11 +195,11 @@ __device__ __forceinline__ int traverse_closest_on(const DevScene &sc, const Tra
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      const bool h0 = slab_hit_child0(r, a, c, closest);
-      const bool h1 = slab_hit_child1(r, b, c, closest);
-      int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+      const bool h0 = slab_hit_child(r, a, b, closest);
+      const bool h1 = slab_hit_child(r, c, d, closest);
+      int r0 = __float_as_int(b.z), r1 = __float_as_int(d.z);
       if (h0 && h1) {
-        const bool f1 = child1_first(d, oct);
+        const bool f1 = child1_first(b, oct);
         const int nearc = f1 ? r1 : r0, farc = f1 ? r0 : r1;
         if (sp >= STACK) {
           atomicOr(err, KERR_STACK_OVERFLOW);
@@ -268,11 +265,11 @@ __device__ __forceinline__ int traverse_spec(const DevScene &sc, const TraceRay 
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      const bool h0 = slab_hit_child0<OCT>(r, a, c, closest);
-      const bool h1 = slab_hit_child1<OCT>(r, b, c, closest);
-      int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+      const bool h0 = slab_hit_child<OCT>(r, a, b, closest);
+      const bool h1 = slab_hit_child<OCT>(r, c, d, closest);
+      int r0 = __float_as_int(b.z), r1 = __float_as_int(d.z);
       if (h0 && h1) {
-        const bool f1 = child1_first(d, oct);
+        const bool f1 = child1_first(b, oct);
         const int nearc = f1 ? r1 : r0, farc = f1 ? r0 : r1;
         if (sp >= STACK) {
           atomicOr(err, KERR_STACK_OVERFLOW);
@@ -362,11 +359,11 @@ __device__ __forceinline__ int traverse_packet(const DevScene &sc, const TraceRa
       const float4 *N = bvh + 4ll * node;
       float4 a, b, c, d;
       load_node(N, a, b, c, d);
-      const bool any0 = __any_sync(0xffffffffu, slab_hit_child0<OCT>(r, a, c, closest));
-      const bool any1 = __any_sync(0xffffffffu, slab_hit_child1<OCT>(r, b, c, closest));
-      const int r0 = __float_as_int(d.x), r1 = __float_as_int(d.y);
+      const bool any0 = __any_sync(0xffffffffu, slab_hit_child<OCT>(r, a, b, closest));
+      const bool any1 = __any_sync(0xffffffffu, slab_hit_child<OCT>(r, c, d, closest));
+      const int r0 = __float_as_int(b.z), r1 = __float_as_int(d.z);
       if (any0 && any1) {
-        const bool f1 = child1_first(d, oct);
+        const bool f1 = child1_first(b, oct);
         if (sp >= STACK) {
           if (lane == 0) atomicOr(err, KERR_STACK_OVERFLOW);
           break;
