@@ -199,10 +199,10 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   loop iteration before the warp's shared leaf pool and
  *                   refill bookkeeping run (1, 2 or 3, default 3)
  *   "trace.wide_min_tris"  scenes with at least this many triangles use
- *                   the 8-wide caster (default 2^17; smaller trees stay in
- *                   cache, where the binary layout is faster); it applies
- *                   to closest-hit casts and to the wavefront render's
- *                   bounce rays alike
+ *                   the 8-wide caster (default 0: every scene; the binary
+ *                   layout is then used for packets only); it applies to
+ *                   closest-hit casts and to the wavefront render's bounce
+ *                   rays alike
  *   "trace.block"   threads per block of the casting kernels: 64, 128
  *                   (default) or 256; the register budget per thread stays
  *                   the one the minblocks keys name

@@ -92,7 +92,7 @@ struct TraceOpts {
   int wide_minblocks = 6;  // resident 128-thread blocks per SM k_trace_wide is compiled for (8, 6 or 5)
   int wide_refill = 4;     // idle lanes of a k_trace_wide warp that trigger a fetch of new rays (1..32)
   int wide_visits = 3;     // node steps per lane per k_trace_wide loop iteration (1..3)
-  uint32_t wide_min_tris = 1u << 17;  // scenes from this many triangles up use the 8-wide caster
+  uint32_t wide_min_tris = 0;  // scenes from this many triangles up use the 8-wide caster
   uint32_t host_chunk = 1u << 21;  // rays per pipelined chunk of rtTraceClosestHost
   int block = 128;  // threads per block of the casting kernels (64, 128 or 256)
   int stack = 0;    // traversal stack entries (16, 32 or 64; 0: the smallest that holds the tree)
