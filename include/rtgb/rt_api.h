@@ -217,7 +217,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   2 (default) wavefront from render.wavefront_pixels up;
  *                   images are identical in every mode
  *   "render.wavefront_pixels"  the mode-2 threshold of rtRender (default
- *                   2^20 pixels)
+ *                   2^18 pixels: 512 x 512 and up)
  *   "render.batch_wavefront_pixels"  the split of batches and of the
  *                   render server's steps: jobs from this many pixels up run
  *                   as wavefronts side by side on side streams, the rest in

@@ -156,7 +156,7 @@ cudaError_t launch_render_wavefront(const DevScene &sc, const rt_camera &cam, co
 // Render launch-shape knobs (rtSetTuning "render.mode").
 struct RenderOpts {
   int mode = 2;                         // 0 megakernel, 1 wavefront, 2 choose by image size
-  uint64_t wavefront_pixels = 1u << 20;  // mode 2: wavefront from this many pixels up
+  uint64_t wavefront_pixels = 1u << 18;  // mode 2: wavefront from this many pixels up
   int batch_streams = 16;                // side streams a batch spreads its wavefront jobs over (1..16)
   // Batches and the render server: jobs from this many pixels up run as
   // wavefronts on side streams (the rest in the persistent tile launch).
