@@ -344,7 +344,7 @@ __host__ __device__ constexpr int pool_entries() {
 constexpr int kFinish = 64;  // finished-ray ring per warp (power of two, >= 64)
 template <int VISITS>
 __host__ __device__ constexpr int wide_warp_smem() {
-  return 64 * 16 + 32 * 8 + 32 * 16 + pool_entries<VISITS>() * 4 + kFinish * 4;
+  return 64 * 16 + 32 * 8 + 32 * 16 + pool_entries<VISITS>() * 4 + kFinish * 4 + 16;
 }
 
 // ref[s] without local memory: a select tree on the bits of s.
@@ -400,8 +400,8 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
                                                                int refill, bool refine) {
   // Per warp (wide_warp_smem bytes, dynamic): the lanes' rays (32 x 2
   // float4), closest-hit keys (32 x u64), winning t/u/v/leaf (32 x float4),
-  // the leaf pool (kPool x u32) and the ring of finished rays waiting for
-  // their fp64 re-evaluation (kFinish x u32).
+  // the leaf pool (kPool x u32), the ring of finished rays waiting for
+  // their fp64 re-evaluation (kFinish x u32) and the pool's tail (16 bytes).
   extern __shared__ float4 s_wide[];
   uint32_t lane;
   asm("mov.u32 %0, %%laneid;" : "=r"(lane));
@@ -415,6 +415,10 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
   float4 *hit_s = wbase + 80;
   uint32_t *pool = reinterpret_cast<uint32_t *>(wbase + 112);
   uint32_t *finish = pool + kPool;
+  // The pool's tail: lanes reserve their entries with one shared atomic.
+  volatile uint32_t *pool_tail = finish + kFinish;
+  if (lane == 0) *pool_tail = 0u;
+  __syncwarp();
   uint32_t fhead = 0, ftail = 0;
   // fp64 re-evaluation of 32 queued finished rays (or the `cnt` left at the
   // end), one per lane: converged, so the few fp64 operations of each ray
@@ -623,17 +627,11 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
         node = __ldg(words8 + 24ll * gnode + 16 + (rk ^ oct));
       }
 
-      // Pool this step's leaves (warp-wide exclusive prefix of the counts).
+      // Pool this step's leaves: each lane reserves its run of entries with
+      // one shared-memory atomic (the pool's order does not matter).
       const uint32_t c = __popc(leafmask);
-      uint32_t incl = c;
-  #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
-      }
-      const uint32_t added = __shfl_sync(0xffffffffu, incl, 31);
       if (c) {
-        uint32_t pos = tail + incl - c;
+        uint32_t pos = atomicAdd(const_cast<uint32_t *>(pool_tail), c);
   #pragma unroll
         for (int s = 0; s < 8; s++) {
           if (!((leafmask >> s) & 1u)) continue;
@@ -643,8 +641,8 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
         }
         mlp1 = pos;
       }
-      tail += added;
       __syncwarp();
+      tail = *pool_tail;
     }
 
     // Leaf rounds: 32 pooled leaves at a time, oldest first.
@@ -737,6 +735,10 @@ cudaError_t launch_wide(const DevScene &sc, const float4 *rays, uint32_t n, int4
                                              : k_trace_wide<GSTACK, 5, false, 1>);
   const size_t smem = (size_t)(block / 32) * (visits >= 2 ? wide_warp_smem<2>() : wide_warp_smem<1>());
   static_assert(wide_warp_smem<3>() == wide_warp_smem<2>(), "visits 2 and 3 share the pool size");
+  if (smem > 48 * 1024) {  // 256-thread blocks with the large pool
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   kern<<<persistent_grid(kern, n, block, smem), block, smem, st>>>(sc, rays, n, nullptr, hits, counter, err, perm,
                                                                    list, list_count, refill, refine);
   return cudaGetLastError();
