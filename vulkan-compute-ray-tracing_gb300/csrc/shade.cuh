@@ -8,6 +8,7 @@
 #include "rt_internal.h"
 #include "rt_math.cuh"
 #include "traverse.cuh"
+#include "wide.cuh"
 
 namespace rtgb {
 
@@ -169,7 +170,10 @@ __device__ __forceinline__ bool closest_hit(const DevScene &sc, const PathState 
     return sphere_pass(sc, ps, o, d, hit, rec);
   }
   TraceRay r = make_ray(o, d, kTmin);
-  int k = traverse_spec<STACK>(sc, r, true, closest, u, v, err);
+  // Bounce rays: per thread over the 8-wide nodes (levels of the fold never
+  // exceed the binary tree's, so STACK group entries suffice).
+  int k = sc.bvh8 ? traverse_wide_lane<STACK>(sc, r, closest, u, v, err)
+                  : traverse_spec<STACK>(sc, r, true, closest, u, v, err);
   return resolve_hit(sc, ps, o, d, k, closest, rec);
 }
 

@@ -20,6 +20,7 @@
 #include "rt_internal.h"
 #include "shade.cuh"
 #include "traverse.cuh"
+#include "wide.cuh"
 
 namespace rtgb {
 namespace {
@@ -278,15 +279,6 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_lanes(DevScene sc, const f
   }
 }
 
-// One bvh8 slot (32 bytes) in one 256-bit load: (lo.x, lo.y, lo.z, hi.x),
-// (hi.y, hi.z, ref, 0). Nodes are 256 bytes and the slab is 256-byte
-// aligned, so every slot is 32-byte aligned.
-__device__ __forceinline__ void load_slot8(const float4 *P, float4 &a, float4 &b) {
-  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-      : "l"(P));
-}
-
 // Ordered keys for (t, triangle) pairs: ord_f maps fp32 to uint32 so that
 // unsigned order equals float order (-0 is first mapped to +0 by the
 // callers, which compare it equal to +0 as floats do).
@@ -316,24 +308,6 @@ __device__ __forceinline__ bool tri_candidate(const float4 *__restrict__ tpre, i
   return !(u < 0.0f || u > 1.0f || v < 0.0f || __fadd_rn(u, v) > 1.0f);
 }
 
-// 2^e as fp32 for e in [-126, 127].
-__device__ __forceinline__ float pow2i(int e) { return __int_as_float((e + 127) << 23); }
-// Byte b of w as the fp32 value 2^23 + byte (exact), assembled by a byte
-// permute; the caster subtracts 2^23 from two such values with one packed
-// instruction, which gives the byte exactly.
-__device__ __forceinline__ float qraw(uint32_t w, int b) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)b));
-}
-
-// Slot-order bits to rank order: bit s moves to bit s ^ oct (three
-// conditional swaps of bit groups).
-__device__ __forceinline__ uint32_t rank_bits(uint32_t x, uint32_t oct) {
-  if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
-  if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
-  if (oct & 4u) x = ((x & 0x0fu) << 4) | ((x >> 4) & 0x0fu);
-  return x;
-}
-
 // Leaf pool entries per warp (power of two): at most 31 are left after the
 // leaf rounds of an iteration, and each of its VISITS node steps adds at
 // most 8 per lane (31 + 3 * 256 < 1024).
@@ -345,14 +319,6 @@ constexpr int kFinish = 64;  // finished-ray ring per warp (power of two, >= 64)
 template <int VISITS>
 __host__ __device__ constexpr int wide_warp_smem() {
   return 64 * 16 + 32 * 8 + 32 * 16 + pool_entries<VISITS>() * 4 + kFinish * 4 + 16;
-}
-
-// ref[s] without local memory: a select tree on the bits of s.
-__device__ __forceinline__ int32_t pick8(const int32_t (&ref)[8], uint32_t s) {
-  const int32_t r01 = (s & 1u) ? ref[1] : ref[0], r23 = (s & 1u) ? ref[3] : ref[2];
-  const int32_t r45 = (s & 1u) ? ref[5] : ref[4], r67 = (s & 1u) ? ref[7] : ref[6];
-  const int32_t r03 = (s & 2u) ? r23 : r01, r47 = (s & 2u) ? r67 : r45;
-  return (s & 4u) ? r47 : r03;
 }
 
 // One ray per lane over bvh8 (Ylitie et al., HPG 2017, with explicit child
@@ -435,7 +401,6 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
     fhead += cnt;
   };
   const float INF = __int_as_float(0x7f800000);
-  const f2 qbias2 = pk2(8388608.0f, 8388608.0f);  // the 2^23 of qraw, twice
   if (d_n) n = min(n, *d_n);
   const uint32_t total = list ? min(*list_count, (n + 31) / 32) * 32u : n;
   const float4 *__restrict__ bvh8 = sc.bvh8;
@@ -536,63 +501,12 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_wide(DevScene sc, const fl
         } else {
           const float closest = ord_inv((uint32_t)(key_v[lane] >> 32));
           const int node_idx = node;
-          const float4 *N = bvh8 + 6ll * node;
-          // The 96-byte quantized node in three 256-bit loads: a child's plane
-          // o + q * 2^e is entered at (o - ray.o) / d + q * (2^e / d), one FMA
-          // per plane on the byte q.
-          float4 q0, q1, q2, q3, q4, q5;
-          load_slot8(N, q0, q1);
-          load_slot8(N + 2, q2, q3);
-          load_slot8(N + 4, q4, q5);
-          const uint32_t ew = __float_as_uint(q0.w);
-          const float sx = r.ix() * pow2i((int)(int8_t)(ew & 0xffu));
-          const float sy = r.iy() * pow2i((int)(int8_t)((ew >> 8) & 0xffu));
-          const float sz = r.iz() * pow2i((int)(int8_t)((ew >> 16) & 0xffu));
-          const float ax = (q0.x - r.o.x) * r.ix(), ay = (q0.y - r.o.y) * r.iy(), az = (q0.z - r.o.z) * r.iz();
-          // Near and far byte words per axis (slots 0-3, 4-7): lo for a
-          // positive 1/d, hi for a negative one.
-          const bool fx = (oct & 1u) != 0, fy = (oct & 2u) != 0, fz = (oct & 4u) != 0;
-          const uint32_t lx0 = __float_as_uint(q1.x), lx1 = __float_as_uint(q1.y);
-          const uint32_t ly0 = __float_as_uint(q1.z), ly1 = __float_as_uint(q1.w);
-          const uint32_t lz0 = __float_as_uint(q2.x), lz1 = __float_as_uint(q2.y);
-          const uint32_t hx0 = __float_as_uint(q2.z), hx1 = __float_as_uint(q2.w);
-          const uint32_t hy0 = __float_as_uint(q3.x), hy1 = __float_as_uint(q3.y);
-          const uint32_t hz0 = __float_as_uint(q3.z), hz1 = __float_as_uint(q3.w);
-          const uint32_t nw[6] = {fx ? hx0 : lx0, fx ? hx1 : lx1, fy ? hy0 : ly0,
-                                  fy ? hy1 : ly1, fz ? hz0 : lz0, fz ? hz1 : lz1};
-          const uint32_t fw[6] = {fx ? lx0 : hx0, fx ? lx1 : hx1, fy ? ly0 : hy0,
-                                  fy ? ly1 : hy1, fz ? lz0 : hz0, fz ? lz1 : hz1};
-          ref[0] = __float_as_int(q4.x), ref[1] = __float_as_int(q4.y), ref[2] = __float_as_int(q4.z);
-          ref[3] = __float_as_int(q4.w), ref[4] = __float_as_int(q5.x), ref[5] = __float_as_int(q5.y);
-          ref[6] = __float_as_int(q5.z), ref[7] = __float_as_int(q5.w);
-          // Per slot and axis, the near and far planes in one packed FMA on
-          // the pair of exact byte values (2^23 + q assembled by a byte
-          // permute, 2^23 subtracted). The nearest entered inner child is
-          // the minimum of keys (entry distance with its low three bits
-          // replaced by the slot), an order within 8 ulps of the distances.
-          const f2 sxx = pk2(sx, sx), syy = pk2(sy, sy), szz = pk2(sz, sz);
-          const f2 axx = pk2(ax, ax), ayy = pk2(ay, ay), azz = pk2(az, az);
-          uint32_t hin = 0;
-          float kbest = INF;
+          WideStep ws;
+          wide_node_test(bvh8, node, r, oct, closest, ws);
   #pragma unroll
-          for (int s = 0; s < 8; s++) {
-            const int w = s >> 2, b = s & 3;
-            const f2 tx = fma2(sub2(pk2(qraw(nw[0 + w], b), qraw(fw[0 + w], b)), qbias2), sxx, axx);
-            const f2 ty = fma2(sub2(pk2(qraw(nw[2 + w], b), qraw(fw[2 + w], b)), qbias2), syy, ayy);
-            const f2 tz = fma2(sub2(pk2(qraw(nw[4 + w], b), qraw(fw[4 + w], b)), qbias2), szz, azz);
-            const float tn = max3f(lo2(tx), lo2(ty), fmaxf(lo2(tz), r.tmin));
-            const float tf = min3f(hi2(tx), hi2(ty), fminf(hi2(tz), closest));
-            if (tn <= tf) {
-              if (ref[s] >= 0) {
-                hin |= 1u << s;
-                kbest = fminf(kbest, __uint_as_float((__float_as_uint(tn) & ~7u) | (uint32_t)s));
-              } else {
-                leafmask |= 1u << s;
-              }
-            }
-          }
-          // An infinite entry distance leaves no usable key: take the lowest slot.
-          const uint32_t nearest = kbest < INF ? (__float_as_uint(kbest) & 7u) : (uint32_t)(__ffs(hin) - 1);
+          for (int k = 0; k < 8; k++) ref[k] = ws.ref[k];
+          leafmask = ws.leafmask;
+          const uint32_t hin = ws.hin, nearest = ws.nearest;
           uint32_t ibits = rank_bits(hin, oct);
           node = -1;
           if (ibits) {
