@@ -669,7 +669,18 @@ def serve_c3(ctx, n_scenes: int, n_requests: int, rates, sides=(256, 512, 1024),
     for rate in rates:
         reqs = wl.request_stream(n_requests, rate, len(specs), sides=sides, spp_max=spp_max)
         for mode, kw in (("continuous", dict(max_active=max_active, spp_per_step=spp_step)),
-                         ("plain", dict(max_active=1, spp_per_step=0))):
+                         ("plain", dict(max_active=1, spp_per_step=0)),
+                         ("plain_one_launch", dict(max_active=1, spp_per_step=0))):
+            # plain: one request at a time with rtRender's split (megakernel
+            # below render.wavefront_pixels, wavefront from there up);
+            # plain_one_launch: one persistent megakernel launch per request
+            # (render.mode 0), the reference's one dispatch per frame.
+            old_mode = ctx.get_tuning("render.mode")
+            old_split = ctx.get_tuning("render.batch_wavefront_pixels")
+            if mode == "plain":
+                ctx.set_tuning("render.batch_wavefront_pixels", ctx.get_tuning("render.wavefront_pixels"))
+            if mode == "plain_one_launch":
+                ctx.set_tuning("render.mode", 0)
             with serve.Server(ctx, hbm_budget_bytes=150 << 30, **kw) as srv:
                 handles = [srv.add_scene(*d) for d in datas]
                 warm = [srv.submit(h, wl.default_camera(8), 8, 8, 1, 1, keep_image=False) for h in handles]
@@ -681,11 +692,19 @@ def serve_c3(ctx, n_scenes: int, n_requests: int, rates, sides=(256, 512, 1024),
                 out[f"{mode}@{rate:g}"] = {"renders_s": len(reqs) / wall, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
                                            "mean_ms": st.mean_ms, "steps": st.steps, "wall_s": wall,
                                            "uploads": st.scene_uploads, "evictions": st.scene_evictions}
+            ctx.set_tuning("render.mode", old_mode)
+            ctx.set_tuning("render.batch_wavefront_pixels", old_split)
     ratios = {f"{r:g}": out[f"continuous@{r:g}"]["renders_s"] / out[f"plain@{r:g}"]["renders_s"] for r in rates}
+    ratios_one = {f"{r:g}": out[f"continuous@{r:g}"]["renders_s"] / out[f"plain_one_launch@{r:g}"]["renders_s"]
+                  for r in rates}
     best = max(v["renders_s"] for k, v in out.items() if k.startswith("continuous"))
     return {"workload": f"served renders: {n_requests} Poisson requests per rate over {len(specs)} resident "
                         f"scenes, sides {tuple(sides)}, spp 1-{spp_max}, 8 bounces, 150 GB budget",
             "value": best, "unit": "renders/s", "rates": out, "speedup_vs_plain": ratios,
+            "speedup_vs_one_launch_per_request": ratios_one,
+            "plain_forms": "plain: one request at a time with rtRender's split (megakernel below 512^2, wavefront "
+                           "from there up); plain_one_launch: one request at a time, one megakernel launch per "
+                           "request",
             "e2e": {"value": best, "unit": "renders/s",
                     "note": "requests submitted from the host with each image copied back to host memory; "
                             "wall clock from the first arrival to the last completion"}}

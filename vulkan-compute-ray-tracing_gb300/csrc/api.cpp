@@ -1001,13 +1001,13 @@ uint64_t scene_device_bytes(uint32_t nt, uint32_t nm, uint32_t nl, uint32_t ns) 
 
 }  // namespace rtgb
 
-// A batch is split by image size the way rtRender chooses its kernels: jobs
-// that rtRender would render with the wavefront kernels (render.mode 1, or
-// 2 and >= 2^20 pixels) run one after another on a side stream through the
-// wavefront path, while one persistent launch covers the tiles of all other
-// jobs on the caller's stream. The two overlap: the small jobs fill the SMs
-// that the wavefront's later, shorter bounces leave idle. Every image equals
-// rtRender of its job alone.
+// A batch is split by image size: jobs from render.batch_wavefront_pixels up
+// (render.mode 2; every job in mode 1, none in mode 0; by default every job)
+// run through the wavefront path, spread over side streams, while one
+// persistent launch covers the tiles of all other jobs on the caller's
+// stream. The two overlap: the small jobs fill the SMs that the wavefront's
+// later, shorter bounces leave idle. Every image equals rtRender of its job
+// alone.
 struct rt_batch {
   BatchJob *d_jobs = nullptr;  // persistent-launch jobs
   uint32_t n = 0, total_tiles = 0, max_depth = 0;
