@@ -2,13 +2,16 @@
 //
 // The tree is the reference's (or the selected builder's) binary tree with
 // levels folded together; no box is recomputed or moved. Each bvh8 node
-// holds up to eight children: starting from one inner node's two children,
-// the inner child with the largest surface area is replaced by its own two
-// children until there are eight or only leaves are left (greedy collapse
-// as in Wald et al., "Getting Rid of Packets", RT 2008, and Ylitie et al.,
-// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
-// BVHs", HPG 2017). A node with fewer than eight children therefore holds
-// leaves only, which bounds the node count by (4n - 1) / 7 for n leaves.
+// holds up to eight children. By default the binary nodes that become bvh8
+// nodes are chosen by the surface area heuristic (the SAH collapse below,
+// the dynamic program of Ylitie et al., "Efficient Incoherent Ray Traversal
+// on GPUs Through Compressed Wide BVHs", HPG 2017, for single-triangle
+// leaves). The alternative ("bvh8.collapse" 0) starts from one inner node's
+// two children and replaces the inner child with the largest surface area
+// by its own two children until there are eight or only leaves are left
+// (greedy collapse as in Wald et al., "Getting Rid of Packets", RT 2008); a
+// node with fewer than eight children then holds leaves only, which bounds
+// the node count by (4n - 1) / 7 for n leaves, the capacity reserved.
 //
 // Slots are assigned by position (Ylitie et al.'s octant order): slot s,
 // read as three bits (x, y, z), stands for the corner of the node on the
