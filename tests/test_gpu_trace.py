@@ -438,3 +438,39 @@ def test_bvh8_collapse_modes_keep_hits(rt, orc, ctx, collapse):
             ctx.set_tuning(k, v)
         for sc in scs:
             sc.release()
+
+
+@pytest.mark.parametrize("builder", [0, 1, 2], ids=["reference", "lbvh", "ploc"])
+def test_degenerate_geometry_both_folds(rt, orc, ctx, builder):
+    """Stacked identical triangles, point-sized (zero-area) triangles and a
+    flat grid: every tree and both 8-wide folds give the oracle's hits (the
+    lowest index among exactly equal t). Zero-area boxes give the SAH fold
+    no preference; where it would need more nodes than the slab reserves,
+    the upload takes the largest-first fold."""
+    t, m, _ = rt.gen_cornell(5, 600, 0)
+    t = t.copy()
+    rng = np.random.default_rng(5)
+    # 200 copies of one triangle, 300 point triangles, the rest as generated.
+    t[12:212, 0:12] = t[12, 0:12]
+    p = rng.uniform(-3, 3, (300, 3)).astype(np.float32)
+    for v in range(3):
+        t[212:512, 4 * v:4 * v + 3] = p
+    keys = ("bvh8.collapse", "trace.wide_min_tris", "bvh.builder")
+    old = [ctx.get_tuning(k) for k in keys]
+    try:
+        ctx.set_tuning("trace.wide_min_tris", 0)
+        ctx.set_tuning("bvh.builder", builder)
+        for collapse in (1, 0):
+            ctx.set_tuning("bvh8.collapse", collapse)
+            sc = ctx.upload_scene(t, m)
+            try:
+                cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, 64, 48)
+                rays = np.concatenate([rt.gen_camera_rays(cam, 64, 48), rt.gen_random_rays(17, 6000, -4.0, 4.0)])
+                want = orc.trace(t, sc.bvh(), rays)
+                got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (builder, collapse)
+            finally:
+                sc.release()
+    finally:
+        for k, v in zip(keys, old):
+            ctx.set_tuning(k, v)

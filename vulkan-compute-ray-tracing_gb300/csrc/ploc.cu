@@ -70,23 +70,35 @@ __global__ void k_ploc_leaves(const rt_triangle *__restrict__ tris, const uint32
   heights[k] = 1;
 }
 
-// Nearest neighbour by merged surface area within the radius (ties: lower
-// index). The area is symmetric in the pair, so following nearest neighbours
-// never increases the area and, with the index tie rule, ends in a mutual
-// pair: every round merges at least one pair.
+// Tie key of the unordered pair (i, j), the same seen from either side:
+// nearer positions first, then pairs starting at an even position (so that a
+// run of equal boxes pairs up as (0, 1), (2, 3), ... and halves each round
+// instead of merging one pair per round into a chain), then the lower start.
+__device__ __forceinline__ unsigned long long pair_key(uint32_t i, uint32_t j) {
+  const uint32_t lo = min(i, j), gap = max(i, j) - lo;
+  return ((unsigned long long)gap << 33) | ((unsigned long long)(lo & 1u) << 32) | lo;
+}
+
+// Nearest neighbour by merged surface area within the radius, equal areas
+// ordered by pair_key. Area and key are symmetric in the pair, so the pair
+// smallest in (area, key) among all is chosen by both its members: every
+// round merges at least one pair.
 __global__ void k_ploc_nearest(const Box *__restrict__ boxes, uint32_t m, uint32_t *nn) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const Box bi = boxes[i];
   float best = __int_as_float(0x7f800000);
+  unsigned long long best_key = ~0ull;
   uint32_t arg = i;
   const uint32_t lo = i > (uint32_t)kRadius ? i - kRadius : 0;
   const uint32_t hi = min(m - 1, i + (uint32_t)kRadius);
   for (uint32_t j = lo; j <= hi; j++) {
     if (j == i) continue;
-    float a = half_area(join(bi, boxes[j]));
-    if (arg == i || a < best) {
+    const float a = half_area(join(bi, boxes[j]));
+    const unsigned long long key = pair_key(i, j);
+    if (arg == i || a < best || (a == best && key < best_key)) {
       best = a;
+      best_key = key;
       arg = j;
     }
   }
