@@ -582,7 +582,7 @@ def large_c4(ctx, frames: int):
                     "d2h_bytes_per_step": W * H * 16 // frames}}
 
 
-def batch_c2(ctx, n_scenes: int, reps: int):
+def batch_c2(ctx, n_scenes: int, reps: int, modes=("plain_one_launch", "plain", "batched", "batched_graph")):
     """256 scenes of uneven size, 4 spp, 8 bounces: the batched launch (one
     persistent launch over the small jobs plus wavefront side streams, and
     its CUDA-graph replay) against one request per launch."""
@@ -623,6 +623,8 @@ def batch_c2(ctx, n_scenes: int, reps: int):
 
     for name, fn in (("plain_one_launch", one_launch), ("plain", plain), ("batched", lambda k: b.launch(sptr)),
                      ("batched_graph", lambda k: b.launch_graph(sptr))):
+        if name not in modes:
+            continue
         fn(0)  # warm-up
         torch.cuda.synchronize()
         ctx.segments(reset=True)
@@ -644,11 +646,12 @@ def batch_c2(ctx, n_scenes: int, reps: int):
     b.destroy()
     for sc in scenes:
         sc.release()
-    best = res["batched_graph"]
+    best = res.get("batched_graph") or res.get("batched") or next(iter(res.values()))
+    ratio = (lambda key: best["renders_s"] / res[key]["renders_s"] if key in res else None)
     return {"workload": f"batched render: {len(jobs)} scenes ({tris_total} triangles), sides 128-1024, 4 spp, "
                         f"8 bounces", "value": best["renders_s"], "unit": "renders/s", "mrays_s": best["mrays_s"],
-            "modes": res, "speedup_vs_one_launch_per_request": best["renders_s"] / res["plain_one_launch"]["renders_s"],
-            "speedup_vs_rtrender_per_request": best["renders_s"] / res["plain"]["renders_s"],
+            "modes": res, "speedup_vs_one_launch_per_request": ratio("plain_one_launch"),
+            "speedup_vs_rtrender_per_request": ratio("plain"),
             "plain_forms": "plain_one_launch: one k_render launch per request, the reference's one dispatch per "
                            "frame; plain: rtRender per request (megakernel below 2^20 pixels, wavefront above)",
             "setup_s": setup_s, "bvh_build_ms_total": build_ms, "reps": reps,
@@ -721,7 +724,7 @@ def run_render(args):
 def run_batch(args):
     import rtgb
     ctx = rtgb.Context(0)
-    r = batch_c2(ctx, args.batch_scenes, max(1, args.steps))
+    r = batch_c2(ctx, args.batch_scenes, max(1, args.steps), tuple(args.batch_modes.split(",")))
     _line(r.pop("workload"), METRIC, r.pop("value"), r.pop("unit"), args, r)
     ctx.close()
 
@@ -777,6 +780,8 @@ def main():
                     help="skip the render, batched, served and large-scene configurations of the default line")
     ap.add_argument("--workload", default="closest-hit", choices=["closest-hit", "render", "batch", "serve", "large"])
     ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-modes", default="plain_one_launch,plain,batched,batched_graph",
+                    help="forms the batch workload times (a subset narrows a profile to the batched launch)")
     ap.add_argument("--serve-scenes", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-rates", default="10,100,2000")
