@@ -322,23 +322,21 @@ __host__ __device__ constexpr int wide_warp_smem() {
 }
 
 // One ray per lane over bvh8 (Ylitie et al., HPG 2017, with explicit child
-// refs). A step loads the lane's 96-byte quantized node (three 256-bit
-// loads) and tests its eight slots. Each axis's near and far planes are
-// picked once per node by the sign of the lane's 1/d (a select on the byte
-// words), so a slot costs six byte decodes, six FMAs and two three-operand
-// min/max; empty slots hold an inverted box (and a harmless leaf ref), so
-// no per-slot mask test is needed. The node's slots were
-// assigned by octant (bvh8.cu), so the entered inner children, kept as the
-// bits s ^ o of a rank mask (o: the sign bits of the ray's direction), come
-// out roughly near-first by taking the lowest set bit — no distance sort.
-// The child with the smallest entry distance (tracked while the slots are
-// tested) is visited next; the node and its other rank bits form a group on
-// the lane's stack (one entry per level at most), and the next child of a
-// group is fetched by re-reading one ref word of its node. On the bench
-// mesh this order visits 8% more nodes than a full sort, at a fraction of
-// its instructions.
+// refs). A step tests the lane's 96-byte quantized node (wide.cuh:
+// wide_node_test: three 256-bit loads, eight slot tests with packed FMAs;
+// empty slots hold an inverted box and a harmless leaf ref, so no per-slot
+// mask test is needed). The node's slots were assigned by octant
+// (bvh8.cu), so the entered inner children, kept as the bits s ^ o of a rank
+// mask (o: the sign bits of the ray's direction), come out roughly
+// near-first by taking the lowest set bit — no distance sort. The child
+// with the smallest entry distance is visited next; the node and its other
+// rank bits form a group on the lane's stack (one entry per level at most),
+// and the next child of a group is fetched by re-reading one ref word of its
+// node. On the bench mesh this order visits 8% more nodes than a full sort,
+// at a fraction of its instructions.
 // Leaves that are hit go to the warp's FIFO leaf pool in shared memory as
-// (leaf, lane) entries; whenever 32 are pooled, or a lane has run out of
+// (leaf, lane) entries, each lane reserving its run with one shared atomic;
+// whenever 32 are pooled, or a lane has run out of
 // nodes with entries still pooled, the 32 lanes test one pooled triangle
 // each against the owning lane's ray (kept in shared memory), so triangle
 // tests run with every lane busy whatever the rays' phases. Each ray's
