@@ -234,6 +234,9 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   the reference's tree, but closest hits are identical
  *                   (equal-t ties go to the lower triangle index in every
  *                   tree); rtDownloadBvh returns the tree that was built
+ *   "bvh.ploc_radius"  positions on either side the PLOC builder
+ *                   (bvh.builder 2) searches for nearest neighbours, 1..256
+ *                   (default 16)
  *   "bvh8.collapse"  how rtUploadScene folds the tree into the 8-wide
  *                   nodes the incoherent caster walks: 1 (default) the
  *                   folded pairs chosen by the surface area heuristic

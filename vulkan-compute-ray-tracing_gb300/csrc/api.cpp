@@ -415,11 +415,12 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   if (nodes) {
     UCK(cudaMemcpyAsync(dnodes, nodes, sizeof(rt_bvh_node) * nnodes, cudaMemcpyHostToDevice, st), "upload nodes");
   } else {
-    int builder = 0, test_error_level = -1;
+    int builder = 0, test_error_level = -1, ploc_radius = 16;
     {
       std::lock_guard<std::mutex> g(ctx->mu);
       builder = ctx->build_opts.builder;
       test_error_level = ctx->build_opts.test_error_level;
+      ploc_radius = ctx->build_opts.ploc_radius;
     }
     char errbuf[256] = {0};
     rt_status bs;
@@ -427,8 +428,8 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
       bs = gpu_build_lbvh((const rt_triangle *)(slab + off_tris), nt, dnodes, st, &sc->build_ms, &depth, errbuf,
                           sizeof(errbuf));
     } else if (builder == 2) {
-      bs = gpu_build_ploc((const rt_triangle *)(slab + off_tris), nt, dnodes, st, &sc->build_ms, &depth, errbuf,
-                          sizeof(errbuf));
+      bs = gpu_build_ploc((const rt_triangle *)(slab + off_tris), nt, (uint32_t)ploc_radius, dnodes, st,
+                          &sc->build_ms, &depth, errbuf, sizeof(errbuf));
     } else {
       std::vector<uint8_t> axes(nnodes);
       glibc_rand_axes(bvh_seed, nnodes, axes.data());
@@ -826,6 +827,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->build_opts.builder = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "bvh.ploc_radius") {
+    if (value < 1 || value > 256) return RT_ERR_INVALID_ARGUMENT;
+    ctx->build_opts.ploc_radius = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "bvh8.collapse") {
     if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
     ctx->build_opts.collapse = (int)value;
@@ -926,6 +932,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "bvh8.collapse") {
     *value = ctx->build_opts.collapse;
+    return RT_SUCCESS;
+  }
+  if (k == "bvh.ploc_radius") {
+    *value = ctx->build_opts.ploc_radius;
     return RT_SUCCESS;
   }
   if (k == "bvh.test_error_level") {

@@ -21,8 +21,6 @@ namespace rtgb {
 
 namespace {
 
-constexpr int kRadius = 16;
-
 struct Box {
   float lo[3], hi[3];
 };
@@ -83,15 +81,15 @@ __device__ __forceinline__ unsigned long long pair_key(uint32_t i, uint32_t j) {
 // ordered by pair_key. Area and key are symmetric in the pair, so the pair
 // smallest in (area, key) among all is chosen by both its members: every
 // round merges at least one pair.
-__global__ void k_ploc_nearest(const Box *__restrict__ boxes, uint32_t m, uint32_t *nn) {
+__global__ void k_ploc_nearest(const Box *__restrict__ boxes, uint32_t m, uint32_t radius, uint32_t *nn) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const Box bi = boxes[i];
   float best = __int_as_float(0x7f800000);
   unsigned long long best_key = ~0ull;
   uint32_t arg = i;
-  const uint32_t lo = i > (uint32_t)kRadius ? i - kRadius : 0;
-  const uint32_t hi = min(m - 1, i + (uint32_t)kRadius);
+  const uint32_t lo = i > radius ? i - radius : 0;
+  const uint32_t hi = min(m - 1, i + radius);
   for (uint32_t j = lo; j <= hi; j++) {
     if (j == i) continue;
     const float a = half_area(join(bi, boxes[j]));
@@ -155,9 +153,9 @@ __global__ void k_ploc_merge(const Box *__restrict__ boxes, const int32_t *__res
 
 }  // namespace
 
-rt_status gpu_build_ploc(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_nodes, cudaStream_t st, float *ms_out,
-                         uint32_t *depth_out, char *errbuf, size_t errlen) {
-  if (n == 0) return RT_ERR_INVALID_ARGUMENT;
+rt_status gpu_build_ploc(const rt_triangle *d_tris, uint32_t n, uint32_t radius, rt_bvh_node *d_nodes,
+                         cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen) {
+  if (n == 0 || radius < 1 || radius > 256) return RT_ERR_INVALID_ARGUMENT;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -204,7 +202,7 @@ rt_status gpu_build_ploc(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_n
       break;
     }
     const uint32_t G = (m + B - 1) / B;
-    k_ploc_nearest<<<G, B, 0, st>>>(boxes[cur], m, nn);
+    k_ploc_nearest<<<G, B, 0, st>>>(boxes[cur], m, radius, nn);
     k_ploc_flags<<<G, B, 0, st>>>(nn, m, keep, merge);
     if ((e = exclusive_scan_u32(keep, keep_pos, sums, m, st)) != cudaSuccess) break;
     if ((e = exclusive_scan_u32(merge, merge_pos, sums, m, st)) != cudaSuccess) break;

@@ -182,6 +182,7 @@ inline bool use_wavefront_batched(const RenderOpts &o, const rt_render_params &p
 struct BuildOpts {
   int builder = 0;  // 0 the reference's Bvh.h tree (bit-exact), 1 LBVH, 2 PLOC
   int collapse = 1;  // 8-wide fold: 1 SAH-chosen pairs, 0 largest child first ("bvh8.collapse")
+  int ploc_radius = 16;  // PLOC's nearest-neighbour search radius ("bvh.ploc_radius")
   int test_error_level = -1;  // test hook of gpu_build_bvh's error word (-1: off)
 };
 
@@ -244,9 +245,10 @@ rt_status gpu_build_lbvh(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_n
 size_t lbvh_sorted_keys_words(uint32_t n);
 cudaError_t lbvh_sorted_keys(const rt_triangle *d_tris, uint32_t n, uint32_t *scratch, uint32_t **codes_out,
                              uint32_t **idx_out, cudaStream_t st);
-// Agglomerative-clustering tree (ploc.cu), Bvh.h node layout, root node 0.
-rt_status gpu_build_ploc(const rt_triangle *d_tris, uint32_t n, rt_bvh_node *d_nodes, cudaStream_t st, float *ms_out,
-                         uint32_t *depth_out, char *errbuf, size_t errlen);
+// Agglomerative-clustering tree (ploc.cu), Bvh.h node layout, root node 0;
+// nearest neighbours searched within `radius` (1..256) positions.
+rt_status gpu_build_ploc(const rt_triangle *d_tris, uint32_t n, uint32_t radius, rt_bvh_node *d_nodes,
+                         cudaStream_t st, float *ms_out, uint32_t *depth_out, char *errbuf, size_t errlen);
 
 // ---------------------------------------------------------------- glibc_rand.cpp
 // glibc's TYPE_3 random() (what rand() returns) after srand(seed).
