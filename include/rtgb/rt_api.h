@@ -157,7 +157,9 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays,
                            uint32_t flags, void *stream);
 /* The same with host arrays: copies in, traces and copies out in pipelined
  * chunks; returns when h_hits is filled. Pinned host memory gives
- * asynchronous DMA. */
+ * asynchronous DMA. Each call uses its own streams and device staging
+ * (from a pool of the context), so calls from several host threads on one
+ * context run side by side. */
 rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_rays, uint32_t n, rt_hit *h_hits);
 
 /* Launch-shape knobs of the context (the reference fixes its launch at

@@ -474,3 +474,39 @@ def test_degenerate_geometry_both_folds(rt, orc, ctx, builder):
     finally:
         for k, v in zip(keys, old):
             ctx.set_tuning(k, v)
+
+
+def test_host_entry_concurrent_calls(rt, ctx):
+    """rtTraceClosestHost from four host threads at once (each call takes
+    its own streams and staging from the context's pool), with chunks small
+    enough that every call pipelines several: every result equals the
+    device-path hits of the same rays, bit for bit."""
+    import threading
+    tris, sc = mesh_scene(rt, ctx, 6, 21)
+    old = ctx.get_tuning("trace.host_chunk")
+    try:
+        ctx.set_tuning("trace.host_chunk", 1 << 16)
+        cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 384, 384)
+        batches = [rt.gen_camera_rays(cam, 384, 384)] + [rt.gen_random_rays(30 + k, 150000) for k in range(3)]
+        want = [gpu_trace(ctx, sc, r) for r in batches]
+        got = [None] * len(batches)
+        errs = []
+
+        def run(k):
+            try:
+                got[k] = sc.trace_host(batches[k])
+            except Exception as e:  # reported below, on the main thread
+                errs.append(e)
+
+        for _ in range(2):
+            ths = [threading.Thread(target=run, args=(k,)) for k in range(len(batches))]
+            for t in ths:
+                t.start()
+            for t in ths:
+                t.join()
+            assert not errs, errs
+            for g, w in zip(got, want):
+                assert np.array_equal(g.view(np.uint32), w.view(np.uint32))
+    finally:
+        ctx.set_tuning("trace.host_chunk", old)
+        sc.release()

@@ -37,10 +37,17 @@ struct Scene {
 
 }  // namespace
 
+// Staging of one rtTraceClosestHost call: two streams whose chunks
+// alternate, each with its own device buffer.
+struct HostLane {
+  cudaStream_t st[2] = {nullptr, nullptr};
+  void *stage[2] = {nullptr, nullptr};
+  size_t bytes = 0;
+};
+
 struct rt_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t aux[2] = {nullptr, nullptr};
   std::mutex mu;
   std::unordered_map<uint32_t, Scene *> scenes;
   uint32_t next_id = 1;
@@ -53,9 +60,9 @@ struct rt_ctx {
   RenderOpts render_opts;
   BuildOpts build_opts;
   uint64_t budget = 0, used = 0, tick = 0;
-  // Device staging for rtTraceClosestHost (two chunk buffers per aux stream).
-  void *stage[2] = {nullptr, nullptr};
-  size_t stage_bytes = 0;
+  // rtTraceClosestHost staging: every lane ever made, and the idle ones
+  // (a call takes one, so calls from several host threads overlap).
+  std::vector<HostLane *> host_lanes, idle_lanes;
 };
 
 namespace {
@@ -198,8 +205,6 @@ rt_status rtCreate(rt_ctx **out, const rt_ctx_desc *desc) {
   ctx->device = desc ? desc->device : 0;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux[0], cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux[1], cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_err, 64);
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 64);
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, sizeof(uint32_t) * kCounterRing);
@@ -225,9 +230,12 @@ rt_status rtDestroy(rt_ctx *ctx) {
     cudaFree(kv.second->slab);
     delete kv.second;
   }
-  for (int i = 0; i < 2; i++) {
-    if (ctx->stage[i]) cudaFree(ctx->stage[i]);
-    if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
+  for (HostLane *l : ctx->host_lanes) {
+    for (int i = 0; i < 2; i++) {
+      if (l->stage[i]) cudaFree(l->stage[i]);
+      if (l->st[i]) cudaStreamDestroy(l->st[i]);
+    }
+    delete l;
   }
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->d_counters) cudaFree(ctx->d_counters);
@@ -638,35 +646,63 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     opts = ctx->trace_opts;
   }
   // Chunks of trace.host_chunk rays alternate between two streams so the
-  // copy of one chunk overlaps the traversal of the other.
+  // copy of one chunk overlaps the traversal of the other. The streams and
+  // buffers are this call's own (a lane of the context's pool), so calls
+  // from several host threads run side by side.
   const uint32_t chunk = opts.host_chunk;
   const size_t io_bytes = (size_t)chunk * (sizeof(rt_ray) + sizeof(rt_hit));
   const size_t chunk_bytes = (trace_chunk_scratch_bytes(chunk) + 255) & ~size_t(255);
   const size_t need = io_bytes + chunk_bytes + raysort_scratch_bytes(chunk);
-  if (ctx->stage_bytes < need) {
-    for (int i = 0; i < 2; i++) {
-      if (ctx->stage[i]) cudaFree(ctx->stage[i]);
-      ctx->stage[i] = nullptr;
-      CK(cudaMalloc(&ctx->stage[i], need), "staging allocation");
+  HostLane *lane = nullptr;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (!ctx->idle_lanes.empty()) {
+      lane = ctx->idle_lanes.back();
+      ctx->idle_lanes.pop_back();
+    } else {
+      lane = new HostLane();
+      ctx->host_lanes.push_back(lane);
     }
-    ctx->stage_bytes = need;
   }
-  for (uint32_t c = 0, k = 0; c < n; c += chunk, k++) {
+  auto give_back = [&] {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->idle_lanes.push_back(lane);
+  };
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 && e == cudaSuccess; i++)
+    if (!lane->st[i]) e = cudaStreamCreateWithFlags(&lane->st[i], cudaStreamNonBlocking);
+  if (e == cudaSuccess && lane->bytes < need) {
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+      if (lane->stage[i]) cudaFree(lane->stage[i]);
+      lane->stage[i] = nullptr;
+      e = cudaMalloc(&lane->stage[i], need);
+    }
+    lane->bytes = e == cudaSuccess ? need : 0;
+  }
+  if (e != cudaSuccess) {
+    give_back();
+    return cuda_fail(ctx, e, "staging allocation");
+  }
+  for (uint32_t c = 0, k = 0; c < n && e == cudaSuccess; c += chunk, k++) {
     uint32_t m = std::min(chunk, n - c);
     int s = k & 1;
-    cudaStream_t st = ctx->aux[s];
-    rt_ray *dr = (rt_ray *)ctx->stage[s];
-    rt_hit *dh = (rt_hit *)((char *)ctx->stage[s] + (size_t)chunk * sizeof(rt_ray));
-    CK(cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st), "rays to device");
+    cudaStream_t st = lane->st[s];
+    rt_ray *dr = (rt_ray *)lane->stage[s];
+    rt_hit *dh = (rt_hit *)((char *)lane->stage[s] + (size_t)chunk * sizeof(rt_ray));
+    e = cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st);
     uint32_t *perm = nullptr;
-    uint32_t *chunks = (uint32_t *)((char *)ctx->stage[s] + io_bytes);
-    if (opts.sort && m >= 65536)
-      CK(launch_raysort(dr, m, nullptr, (char *)ctx->stage[s] + io_bytes + chunk_bytes, &perm, st), "ray sort");
-    CK(launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm, chunks), "trace launch");
-    CK(cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st), "hits to host");
+    uint32_t *chunks = (uint32_t *)((char *)lane->stage[s] + io_bytes);
+    if (e == cudaSuccess && opts.sort && m >= 65536)
+      e = launch_raysort(dr, m, nullptr, (char *)lane->stage[s] + io_bytes + chunk_bytes, &perm, st);
+    if (e == cudaSuccess) e = launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm, chunks);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st);
   }
-  CK(cudaStreamSynchronize(ctx->aux[0]), "trace");
-  CK(cudaStreamSynchronize(ctx->aux[1]), "trace");
+  // Wait for everything queued, also after an error, before the lane is
+  // handed to another call.
+  const cudaError_t e0 = cudaStreamSynchronize(lane->st[0]), e1 = cudaStreamSynchronize(lane->st[1]);
+  give_back();
+  if (e == cudaSuccess) e = e0 != cudaSuccess ? e0 : e1;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "trace");
   return rtSynchronize(ctx, nullptr);
 }
 

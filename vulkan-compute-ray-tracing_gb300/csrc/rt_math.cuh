@@ -61,16 +61,8 @@ __device__ __forceinline__ f2 pk2(float lo, float hi) {
   asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
   return r;
 }
-__device__ __forceinline__ float lo2(f2 a) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-  return lo;
-}
-__device__ __forceinline__ float hi2(f2 a) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-  return hi;
-}
+__device__ __forceinline__ float lo2(f2 a) { return __uint_as_float((uint32_t)a.v); }
+__device__ __forceinline__ float hi2(f2 a) { return __uint_as_float((uint32_t)(a.v >> 32)); }
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
   f2 d;
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.v) : "l"(a.v), "l"(b.v), "l"(c.v));
