@@ -64,7 +64,7 @@ ALG_BYTES_INCOHERENT = 48.0 * (370.590 + 41.355) + 48.0
 RAYS_PER_BATCH = 2048 * 2048
 TUNING_KEYS = ("trace.block", "trace.stack", "trace.sort", "trace.packet", "trace.packet_minblocks", "trace.defer",
                "trace.wide", "trace.wide_minblocks", "trace.wide_visits", "trace.wide_refill", "trace.minblocks",
-               "trace.spec")
+               "trace.spec", "render.sort")
 
 
 def measured_peak_hbm():

@@ -169,7 +169,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *   "trace.sort"    1 (default) = cast batches of >= 65536 rays in Morton
  *                   order of origin and direction (hits still land at their
  *                   ray's input index; scratch comes from the stream-ordered
- *                   pool); also reorders each bounce of a wavefront render
+ *                   pool)
  *   "trace.packet"  1 (default) = a warp whose 32 rays share an origin and
  *                   point within ~18 degrees traverses them as one packet
  *                   (one node sequence, every lane busy); 0 = always one
@@ -228,6 +228,11 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   render alone keeps render.wavefront_pixels)
  *   "render.batch_streams"  side streams a batch (rtBatchCreate) spreads
  *                   its wavefront jobs over, 1..16 (default 16)
+ *   "render.sort"   1 = reorder each bounce's rays of a wavefront render
+ *                   (rtRender, batches, the render server) in Morton order
+ *                   of origin and direction before casting them; 0 (default)
+ *                   = cast them in the order shading queued them, which the
+ *                   8-wide caster takes faster. Images are identical either way
  *   "bvh.builder"   tree built by rtUploadScene when no nodes are given:
  *                   0 (default) the reference's Bvh.h tree, node-for-node;
  *                   1 a linear BVH over Morton-ordered centroids,

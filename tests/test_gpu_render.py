@@ -127,20 +127,20 @@ def test_render_without_camera_is_an_error(rt, ctx):
 @pytest.mark.parametrize("flags,spheres,spp", [(0, 6, 3), ("LEN1", 6, 2), ("SPHERE_OVERRIDE", 6, 1),
                                                ("NO_SPHERES", 0, 2), ("UNORM8", 3, 3), ("SHADE_SIMPLE", 3, 1)])
 def test_wavefront_equals_megakernel(rt, ctx, flags, spheres, spp):
-    """The wavefront split (with per-bounce Morton reordering, bounce rays
-    cast in place or by the 8-wide caster) gives the megakernel's image bit
-    for bit, and counts the same segments."""
+    """The wavefront split (bounce rays with or without per-bounce Morton
+    reordering, cast in place or by the 8-wide caster) gives the
+    megakernel's image bit for bit, and counts the same segments."""
     import torch
     f = 0 if flags == 0 else (getattr(rt, "COMPAT_" + flags, None) or getattr(rt, flags))
     t, m, s, sc = cornell(rt, ctx, n_soup=5000, n_spheres=spheres, seed=6)
-    keys = ("render.mode", "trace.wide", "trace.wide_min_tris")
+    keys = ("render.mode", "trace.wide", "trace.wide_min_tris", "render.sort")
     try:
         W, H = 160, 120
         cam = rt.camera_look_at([0, 0, -14], [0, 0, 0], [0, 1, 0], 40.0, W, H)
         out = {}
         old = [ctx.get_tuning(k) for k in keys]
         try:
-            for shape in ((0, 0, 0), (1, 0, 0), (1, 1, 0)):
+            for shape in ((0, 0, 0, 0), (1, 0, 0, 1), (1, 1, 0, 1), (1, 0, 0, 0), (1, 1, 0, 0)):
                 for k, v in zip(keys, shape):
                     ctx.set_tuning(k, v)
                 ctx.segments(reset=True)
@@ -149,8 +149,8 @@ def test_wavefront_equals_megakernel(rt, ctx, flags, spheres, spp):
         finally:
             for k, v in zip(keys, old):
                 ctx.set_tuning(k, v)
-        base = out[(0, 0, 0)]
-        for shape in ((1, 0, 0), (1, 1, 0)):
+        base = out[(0, 0, 0, 0)]
+        for shape in ((1, 0, 0, 1), (1, 1, 0, 1), (1, 0, 0, 0), (1, 1, 0, 0)):
             assert np.array_equal(base[0].view(np.uint32), out[shape][0].view(np.uint32)), shape
             assert base[1] == out[shape][1], shape
     finally:

@@ -737,7 +737,7 @@ rt_status rtRender(rt_ctx *ctx, rt_scene_id id, const rt_render_params *p, float
     void *scratch = nullptr;
     CK(cudaMallocAsync(&scratch, wavefront_scratch_bytes((uint32_t)pixels), st), "wavefront scratch");
     cudaError_t e = launch_render_wavefront(d, cam, *p, accum, ctx->d_segments, next_counter(ctx), ctx->d_err, scratch,
-                                            topts.sort != 0, use_wide(topts, d), st);
+                                            ropts.sort != 0, use_wide(topts, d), st);
     cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render launch");
     return RT_SUCCESS;
@@ -858,6 +858,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->render_opts.mode = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "render.sort") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->render_opts.sort = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "bvh.builder") {
     if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
     ctx->build_opts.builder = (int)value;
@@ -936,6 +941,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "render.mode") {
     *value = ctx->render_opts.mode;
+    return RT_SUCCESS;
+  }
+  if (k == "render.sort") {
+    *value = ctx->render_opts.sort;
     return RT_SUCCESS;
   }
   if (k == "trace.block") {
@@ -1036,7 +1045,7 @@ int ctx_device(rt_ctx *ctx) { return ctx->device; }
 cudaStream_t ctx_stream(rt_ctx *ctx) { return ctx->stream; }
 bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort, bool *wide, uint32_t *min_tris) {
   std::lock_guard<std::mutex> g(ctx->mu);
-  if (sort) *sort = ctx->trace_opts.sort != 0;
+  if (sort) *sort = ctx->render_opts.sort != 0;
   if (wide) *wide = ctx->trace_opts.wide != 0;
   if (min_tris) *min_tris = ctx->trace_opts.wide_min_tris;
   return use_wavefront_batched(ctx->render_opts, p);
@@ -1065,7 +1074,7 @@ struct rt_batch {
   static constexpr int kSides = 16;
   int sides = 0;
   void *wf_scratch[kSides] = {};
-  bool wf_sort = true;
+  bool wf_sort = false;
   bool wf_wide = true;
   uint32_t wf_wide_min = 0;
   uint32_t *counter = nullptr; // [0] tile counter
@@ -1187,7 +1196,7 @@ rt_status rtBatchCreate(rt_ctx *ctx, const rt_render_job *jobs, uint32_t n_jobs,
   (void)depth;
   b->n = (uint32_t)tiles_jobs.size();
   b->total_tiles = (uint32_t)tiles;
-  b->wf_sort = topts.sort != 0;
+  b->wf_sort = ropts.sort != 0;
   b->wf_wide = topts.wide != 0;
   b->wf_wide_min = topts.wide_min_tris;
   cudaError_t e = cudaMalloc((void **)&b->d_jobs, sizeof(BatchJob) * std::max(b->n, 1u));

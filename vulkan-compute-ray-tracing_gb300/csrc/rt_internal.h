@@ -160,10 +160,16 @@ struct RenderOpts {
   int batch_streams = 16;                // side streams a batch spreads its wavefront jobs over (1..16)
   // Batches and the render server: jobs from this many pixels up run as
   // wavefronts on side streams (the rest in the persistent tile launch).
-  // Jobs that run side by side keep the GPU busy at any size, and sorted
-  // bounce rays beat the megakernel's diverged lanes, so all of them do by
-  // default; a render alone keeps wavefront_pixels.
+  // Jobs that run side by side keep the GPU busy at any size, and queued
+  // bounce rays in the 8-wide caster beat the megakernel's diverged lanes,
+  // so all of them do by default; a render alone keeps wavefront_pixels.
   uint64_t batch_wavefront_pixels = 1;
+  // Wavefront renders: reorder each bounce's rays by Morton key of origin and
+  // direction before casting them (1) or cast them in queue order (0). The
+  // queue keeps the shading warps' order, which is close to the camera
+  // tiles' order, and the 8-wide caster takes them faster unsorted; the
+  // closest-hit entry points keep trace.sort.
+  int sort = 0;
 };
 // True when a render of these params goes to the wavefront kernels.
 inline bool use_wavefront(const RenderOpts &o, const rt_render_params &p) {

@@ -3,17 +3,18 @@
 //
 //   raygen      one path per pixel for sample s (colour 1, the pixel's RNG
 //               seed, the normalised camera ray) -> queue 0
-//   per bounce  [Morton reorder of the queue's rays] -> extend (closest
+//   per bounce  [Morton reorder of the queue's rays, render.sort] -> extend (closest
 //               triangle per ray) -> shade (record, spheres, scatter, colour;
 //               surviving paths are compacted into the other queue)
 //   accumulate  the running mean of comp:375-377 for sample s
 //
 // Every floating-point step is the megakernel's (shade.cuh); only the order
 // in which paths are processed changes, so images are identical to the
-// megakernel's. What the split buys: each bounce's rays are cast in Morton
-// order (secondary rays are otherwise incoherent within a warp), finished
-// paths leave the queue instead of idling lanes, and the casting kernel runs
-// without the shading code's registers. Queue lengths stay on the device;
+// megakernel's. What the split buys: finished paths leave the queue instead
+// of idling lanes, the casting kernel runs without the shading code's
+// registers, and each bounce's rays reach the 8-wide caster, whose warps
+// refill from the queue (in the order shading queued them, or in Morton
+// order when render.sort is set). Queue lengths stay on the device;
 // kernels are sized for the queue's capacity and read the live count, so a
 // render is a fixed launch sequence (no host synchronisation, capturable in
 // a CUDA graph).
