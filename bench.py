@@ -62,7 +62,8 @@ WORKLOAD = "closest-hit, icosphere L8 (1,310,720 tris), 4,194,304 coherent + 4,1
 ALG_BYTES_COHERENT = 48.0 * (530.158 + 61.469) + 48.0
 ALG_BYTES_INCOHERENT = 48.0 * (370.590 + 41.355) + 48.0
 RAYS_PER_BATCH = 2048 * 2048
-TUNING_KEYS = ("trace.block", "trace.stack", "trace.sort", "trace.packet", "trace.packet_minblocks", "trace.defer",
+TUNING_KEYS = ("trace.block", "trace.stack", "trace.sort", "trace.packet", "trace.beam", "trace.packet_minblocks",
+               "trace.defer",
                "trace.wide", "trace.wide_minblocks", "trace.wide_visits", "trace.wide_refill", "trace.minblocks",
                "trace.spec", "render.sort")
 
@@ -324,6 +325,9 @@ def run_gpu(args):
     import rtgb
     tris, mats, coherent, incoherent = make_workload(rtgb)
     ctx = rtgb.Context(local)
+    for kv in args.tuning:
+        key, value = kv.split("=", 1)
+        ctx.set_tuning(key, int(value))
     sc = ctx.upload_scene(tris, mats)
     info = sc.info()
     # A dedicated stream: every launch and every CUDA event of the timed
@@ -813,6 +817,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--closest-hit-only", action="store_true",
                     help="skip the render, batched, served and large-scene configurations of the default line")
+    ap.add_argument("--tuning", action="append", default=[], metavar="KEY=VALUE",
+                    help="closest-hit workload: set a tuning key (rtSetTuning) before the scene upload; repeatable")
     ap.add_argument("--workload", default="closest-hit", choices=["closest-hit", "render", "batch", "serve", "large"])
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-modes", default="plain_one_launch,plain,batched,batched_graph",

@@ -145,6 +145,26 @@ def test_trace_config1_full_batch_vs_oracle(rt, orc, ctx, big_mesh, config1_orac
         assert (got[hit, 1] > 0.999e-4).all() and (got[hit, 1] < 1e4).all()
 
 
+def test_trace_config1_beams_full_batch(rt, ctx, big_mesh, config1_oracle):
+    """Beam casts (trace.beam) of the full coherent batch: every ray's hit
+    index equals the oracle's outside ties, and the hits equal the packet
+    cast's bit for bit."""
+    tris, sc = big_mesh
+    _, batches = config1_oracle
+    rays, want, ties = batches["coherent"]
+    old = ctx.get_tuning("trace.beam")
+    try:
+        ctx.set_tuning("trace.beam", 0)
+        packets = gpu_trace(ctx, sc, rays)
+        ctx.set_tuning("trace.beam", 1)
+        got = gpu_trace(ctx, sc, rays)
+    finally:
+        ctx.set_tuning("trace.beam", old)
+    gi, wi = got.view(np.int32)[:, 0], want.view(np.int32)[:, 0]
+    assert int(((gi != wi) & ~ties).sum()) == 0
+    assert np.array_equal(got.view(np.uint32), packets.view(np.uint32))
+
+
 @pytest.mark.parametrize("builder", [1, 2])
 def test_trace_config1_full_batch_other_trees(rt, ctx, big_mesh, config1_oracle, builder):
     """The LBVH and PLOC trees are quoted on this mesh too: every ray's hit
@@ -236,19 +256,21 @@ def test_invalid_scenes_are_rejected(rt, ctx):
     sc.release()
 
 
-KEYS = ("trace.refill", "trace.sort", "trace.packet", "trace.spec", "trace.wide")
+KEYS = ("trace.refill", "trace.sort", "trace.packet", "trace.spec", "trace.wide", "trace.beam")
 
 
-@pytest.mark.parametrize("refill,sort,packet,spec,wide", [
-    (1, 0, 0, 0, 0), (4, 0, 0, 0, 0), (16, 0, 0, 0, 0), (32, 1, 0, 0, 0), (4, 1, 0, 0, 0), (32, 1, 1, 0, 0),
-    (32, 0, 1, 0, 0), (32, 0, 0, 1, 0), (32, 1, 0, 1, 0), (32, 1, 1, 1, 0), (32, 0, 0, 0, 1), (32, 1, 0, 0, 1),
-    (32, 0, 1, 0, 1), (32, 1, 1, 1, 1)])
-def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wide):
+@pytest.mark.parametrize("refill,sort,packet,spec,wide,beam", [
+    (1, 0, 0, 0, 0, 0), (4, 0, 0, 0, 0, 0), (16, 0, 0, 0, 0, 0), (32, 1, 0, 0, 0, 0), (4, 1, 0, 0, 0, 0),
+    (32, 1, 1, 0, 0, 0), (32, 1, 1, 0, 0, 1), (32, 0, 1, 0, 0, 0), (32, 0, 1, 0, 0, 1), (32, 0, 0, 1, 0, 0),
+    (32, 1, 0, 1, 0, 0), (32, 1, 1, 1, 0, 1), (32, 0, 0, 0, 1, 0), (32, 1, 0, 0, 1, 0), (32, 0, 1, 0, 1, 0),
+    (32, 0, 1, 0, 1, 1), (32, 1, 1, 1, 1, 0), (32, 1, 1, 1, 1, 1)])
+def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wide, beam):
     """Every launch shape of the caster (refill threshold, Morton order,
-    packet traversal of coherent warps, postponed leaves, the 8-wide tree
-    with the warp leaf pool) returns the same results in input order, bit for bit:
-    the visiting order differs between shapes, and equal-t candidates are
-    resolved by leaf index, not by the order met."""
+    packet traversal of coherent warps, beams over 256-ray tiles of one
+    origin, postponed leaves, the 8-wide tree with the warp leaf pool)
+    returns the same results in input order, bit for bit: the visiting order
+    differs between shapes, and equal-t candidates are resolved by leaf
+    index, not by the order met."""
     tris, sc = mesh_scene(rt, ctx, 6, 7)
     old_min = ctx.get_tuning("trace.wide_min_tris")
     ctx.set_tuning("trace.wide_min_tris", 0)  # this 81,920-triangle mesh takes the 8-wide caster too
@@ -256,10 +278,10 @@ def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wid
         cam = rt.camera_look_at([0, 0, -3], [0, 0, 0], [0, 1, 0], 40.0, 256, 200)
         rays = np.concatenate([rt.gen_camera_rays(cam, 256, 200), rt.gen_random_rays(11, 40000)])
         old = [ctx.get_tuning(k) for k in KEYS]
-        for k, v in zip(KEYS, (32, 0, 0, 0, 0)):
+        for k, v in zip(KEYS, (32, 0, 0, 0, 0, 0)):
             ctx.set_tuning(k, v)
         base = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
-        for k, v in zip(KEYS, (refill, sort, packet, spec, wide)):
+        for k, v in zip(KEYS, (refill, sort, packet, spec, wide, beam)):
             ctx.set_tuning(k, v)
         try:
             got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
@@ -275,6 +297,83 @@ def test_trace_launch_shapes_agree(rt, orc, ctx, refill, sort, packet, spec, wid
         sc.release()
 
 
+def beam_ray_sets(rt):
+    """Same-origin ray sets that take the beam path (sorted batches of at
+    least 65,536 rays), and its edges."""
+    def cam(eye, target, up, fov, w, h):
+        return rt.gen_camera_rays(rt.camera_look_at(eye, target, up, fov, w, h), w, h)
+    axis = cam([0, 0, -3], [0, 0, 0], [0, 1, 0], 30.0, 256, 256)  # centre rays with zero x or y
+    neg_x = cam([3, 0.1, 0.2], [0, 0, 0], [0, 1, 0], 35.0, 320, 256)  # dominant axis -x
+    inside = cam([0, 0, 0], [0, 1, 0], [0, 0, 1], 60.0, 256, 256)  # origin inside the mesh, +y
+    grazing = cam([0, 1.25, -3], [0, 1.0, 0], [0, 1, 0], 6.0, 256, 256)  # the silhouette
+    diagonal = cam([2, 2, -2], [0, 0, 0], [0, 1, 0], 70.0, 256, 256)  # dominant axis changes across the image
+    tail = np.concatenate([axis, axis[:37]])  # a partial last tile
+    bounds = axis.copy()
+    bounds[::3, 7] = np.inf  # unbounded rays
+    bounds[1::7, 7] = 0.0  # tmax below tmin: no hit
+    bounds[2::5, 7] = 3.0  # short rays
+    mixed = axis.copy()
+    mixed[1::2, :3] += np.float32(1e-3)  # two origins: no beam
+    stray = axis.copy()
+    stray[5::97, :3] += np.float32(1e-3)  # a few other origins: the sort's sample may miss them
+    wide = cam([0, 0, -3], [0, 0, 0], [0, 1, 0], 150.0, 256, 256)  # tiles too wide for a beam
+    return {"axis": axis, "neg_x": neg_x, "inside": inside, "grazing": grazing, "diagonal": diagonal, "tail": tail,
+            "bounds": bounds, "mixed": mixed, "stray": stray, "wide": wide}
+
+
+@pytest.mark.parametrize("name", ["axis", "neg_x", "inside", "grazing", "diagonal", "tail", "bounds", "mixed",
+                                  "stray", "wide"])
+def test_beam_tiles_equal_packets(rt, orc, ctx, name):
+    """Beams over the ray sort's cell tiles return the packet and per-lane
+    casts' hits bit for bit, on the edges of the beam path: axis-aligned
+    and negative dominant directions, an origin inside the tree's boxes,
+    rays along the silhouette, a dominant axis that changes across the
+    image, a partial last tile, unbounded, empty and short rays, batches
+    of two origins or a few stray ones, and tiles too wide for a beam."""
+    tris, sc = mesh_scene(rt, ctx, 6, 7)
+    rays = beam_ray_sets(rt)[name]
+    keys = ("trace.beam", "trace.sort", "trace.packet")
+    old = [ctx.get_tuning(k) for k in keys]
+    try:
+        ctx.set_tuning("trace.packet", 0)
+        ctx.set_tuning("trace.beam", 0)
+        ctx.set_tuning("trace.sort", 0)
+        want = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+        ctx.set_tuning("trace.packet", 1)
+        for sort in (0, 1):
+            for beam in (0, 1):
+                ctx.set_tuning("trace.sort", sort)
+                ctx.set_tuning("trace.beam", beam)
+                got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (sort, beam)
+        host = sc.trace_host(rays)
+        assert np.array_equal(host.view(np.uint32), gpu_trace(ctx, sc, rays).view(np.uint32))
+    finally:
+        for k, v in zip(keys, old):
+            ctx.set_tuning(k, v)
+        sc.release()
+
+
+def test_beam_tiles_vs_oracle(rt, orc, ctx):
+    """Beam casts of camera tiles against the oracle's culled traversal of
+    the same tree: hit index equal outside exact t ties, t/u/v bit-exact
+    where the index agrees."""
+    tris, sc = mesh_scene(rt, ctx, 6, 7)
+    old = ctx.get_tuning("trace.beam")
+    try:
+        ctx.set_tuning("trace.beam", 1)
+        sets = beam_ray_sets(rt)
+        for name in ("axis", "neg_x", "grazing", "inside"):
+            rays = sets[name]
+            got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+            want, st = orc.trace(tris, sc.bvh(), rays, stats=True)
+            ties = (st[:, 2] & 1) != 0
+            compare(got, want, ties)
+    finally:
+        ctx.set_tuning("trace.beam", old)
+        sc.release()
+
+
 def test_single_triangle_scene(rt, orc, ctx):
     """A one-triangle scene: the root itself is a leaf, in every traversal."""
     t, m, _ = rt.gen_cornell(1, 0)
@@ -284,14 +383,17 @@ def test_single_triangle_scene(rt, orc, ctx):
     old_min = ctx.get_tuning("trace.wide_min_tris")
     ctx.set_tuning("trace.wide_min_tris", 0)
     try:
-        cam = rt.camera_look_at([0, 0, -14], [0, -4, 0], [0, 1, 0], 60.0, 64, 64)
-        rays = rt.gen_camera_rays(cam, 64, 64)
-        want = orc.trace(t, sc.bvh(), rays)
-        for spec, wide in ((0, 0), (1, 0), (0, 1)):
-            ctx.set_tuning("trace.spec", spec)
-            ctx.set_tuning("trace.wide", wide)
-            got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
-            np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        # 60 degrees: tiles too wide for a beam; 8 degrees: every tile a beam.
+        for fov in (60.0, 8.0):
+            cam = rt.camera_look_at([0, 0, -14], [0, -4, 0], [0, 1, 0], fov, 64, 64)
+            rays = rt.gen_camera_rays(cam, 64, 64)
+            want = orc.trace(t, sc.bvh(), rays)
+            for spec, wide, beam in ((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1)):
+                ctx.set_tuning("trace.spec", spec)
+                ctx.set_tuning("trace.wide", wide)
+                ctx.set_tuning("trace.beam", beam)
+                got = gpu_trace(ctx, sc, rays, flags=rt.HIT_FP32)
+                np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
     finally:
         for k, v in zip(KEYS, old):
             ctx.set_tuning(k, v)
@@ -353,7 +455,7 @@ def test_autotune_trace_keeps_hits(rt, orc, ctx):
     """The autotuner's candidates are timing choices only: after tuning, the
     hits equal the ones cast with the settings it started from."""
     keys = ("trace.block", "trace.stack", "trace.wide", "trace.wide_minblocks", "trace.wide_visits", "trace.defer",
-            "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort")
+            "trace.spec", "trace.minblocks", "trace.packet_minblocks", "trace.sort", "trace.beam")
     old = [ctx.get_tuning(k) for k in keys]
     tris, sc = mesh_scene(rt, ctx, 6, 3)
     try:

@@ -620,10 +620,14 @@ rt_status rtTraceClosestEx(rt_ctx *ctx, rt_scene_id id, const rt_ray *rays, uint
   CK(cudaMallocAsync((void **)&scratch, chunk_bytes + (use_sort ? raysort_scratch_bytes(n) : 0), st),
      "trace scratch");
   uint32_t *perm = nullptr;
-  cudaError_t e = use_sort ? launch_raysort(rays, n, nullptr, scratch + chunk_bytes, &perm, st) : cudaSuccess;
+  RayCells cells;
+  const bool beams = use_sort && opts.packet && opts.beam;
+  cudaError_t e = use_sort ? launch_raysort(rays, n, nullptr, scratch + chunk_bytes, &perm, st,
+                                            beams ? &cells : nullptr)
+                           : cudaSuccess;
   if (e == cudaSuccess)
     e = launch_trace(d, rays, n, hits, next_counter(ctx), ctx->d_err, refine, opts, st, perm,
-                     reinterpret_cast<uint32_t *>(scratch));
+                     reinterpret_cast<uint32_t *>(scratch), beams ? &cells : nullptr);
   cudaFreeAsync(scratch, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
   return RT_SUCCESS;
@@ -692,9 +696,14 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id id, const rt_ray *h_rays, 
     e = cudaMemcpyAsync(dr, h_rays + c, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, st);
     uint32_t *perm = nullptr;
     uint32_t *chunks = (uint32_t *)((char *)lane->stage[s] + io_bytes);
-    if (e == cudaSuccess && opts.sort && m >= 65536)
-      e = launch_raysort(dr, m, nullptr, (char *)lane->stage[s] + io_bytes + chunk_bytes, &perm, st);
-    if (e == cudaSuccess) e = launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm, chunks);
+    RayCells cells;
+    const bool sorted = opts.sort && m >= 65536, beams = sorted && opts.packet && opts.beam;
+    if (e == cudaSuccess && sorted)
+      e = launch_raysort(dr, m, nullptr, (char *)lane->stage[s] + io_bytes + chunk_bytes, &perm, st,
+                         beams ? &cells : nullptr);
+    if (e == cudaSuccess)
+      e = launch_trace(d, dr, m, dh, next_counter(ctx), ctx->d_err, true, opts, st, perm, chunks,
+                       beams ? &cells : nullptr);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_hits + c, dh, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, st);
   }
   // Wait for everything queued, also after an error, before the lane is
@@ -776,6 +785,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
   if (k == "trace.packet") {
     if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.packet = (int)value;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.beam") {
+    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.beam = (int)value;
     return RT_SUCCESS;
   }
   if (k == "trace.spec") {
@@ -901,6 +915,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.packet") {
     *value = ctx->trace_opts.packet;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.beam") {
+    *value = ctx->trace_opts.beam;
     return RT_SUCCESS;
   }
   if (k == "trace.spec") {

@@ -6,7 +6,8 @@
 //                64/128/256), trace.stack (traversal stack entries 16/32/64,
 //                each raised to the smallest size that holds the tree),
 //                trace.wide, trace.wide_minblocks, trace.wide_visits, trace.defer, trace.spec,
-//                trace.minblocks, trace.packet_minblocks and trace.sort,
+//                trace.minblocks, trace.packet_minblocks, trace.sort and
+//                trace.beam,
 //                each candidate timed with CUDA events over `reps` casts
 //                after one warm-up cast;
 //   render       megakernel against wavefront at growing square image sizes
@@ -99,7 +100,8 @@ rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, 
                         {"trace.spec", {1, 0}},
                         {"trace.minblocks", {16, 12, 10}},
                         {"trace.packet_minblocks", {16, 12, 10}},
-                        {"trace.sort", {1, 0}}};
+                        {"trace.sort", {1, 0}},
+                        {"trace.beam", {0, 1}}};
   float best = 0.0f;
   rt_status s = time_trace(ctx, scene, d_rays, n, d_hits, reps, &best);
   if (s != RT_SUCCESS) return s;

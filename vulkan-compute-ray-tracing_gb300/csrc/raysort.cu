@@ -143,15 +143,56 @@ __global__ void k_init_ext(uint32_t *ext) {
   }
 }
 
+// Cells: runs of 64 consecutive buckets (a Morton-aligned 8 x 8 block of
+// direction buckets in a one-origin batch). After the scatter hist[k] is
+// one past bucket k's last sorted position, so cell c spans
+// [hist[64c - 1], hist[64c + 63]). Each cell is cut into tiles of at most
+// kTileRays rays.
+constexpr uint32_t kCellBuckets = 64;
+constexpr uint32_t kCells = kBuckets / kCellBuckets;
+constexpr uint32_t kTileRays = 256;
+
+__device__ __forceinline__ void cell_span(const uint32_t *hist, uint32_t c, uint32_t &b, uint32_t &e) {
+  b = c ? hist[c * kCellBuckets - 1] : 0u;
+  e = hist[c * kCellBuckets + kCellBuckets - 1];
+}
+
+__global__ void k_cell_count(const uint32_t *__restrict__ hist, uint32_t *cnt) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= kCells) return;
+  uint32_t b, e;
+  cell_span(hist, c, b, e);
+  cnt[c] = (e - b + kTileRays - 1) / kTileRays;
+}
+
+__global__ void k_cell_emit(const uint32_t *__restrict__ hist, const uint32_t *__restrict__ cnt,
+                            const uint32_t *__restrict__ off, uint32_t *tiles, uint32_t *count) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= kCells) return;
+  uint32_t b, e;
+  cell_span(hist, c, b, e);
+  for (uint32_t j = 0; j < cnt[c]; j++) {
+    const uint32_t t0 = b + j * kTileRays;
+    tiles[2 * (off[c] + j)] = t0;
+    tiles[2 * (off[c] + j) + 1] = min(t0 + kTileRays, e);
+  }
+  if (c == kCells - 1) *count = off[c] + cnt[c];
+}
+
+size_t cell_words(uint32_t n) {
+  // counts | offsets | scan sums | tile count | tiles (at most one partial per cell)
+  return 2ull * kCells + (kCells / 1024 + 2) + 1 + 2ull * (kCells + n / kTileRays + 1);
+}
+
 }  // namespace
 
 size_t raysort_scratch_bytes(uint32_t n) {
-  // ext (16 words) | keys n | hist kBuckets | scan sums | perm n
-  return 4ull * (16 + n + kBuckets + (kBuckets / 1024 + 2) + n);
+  // ext (16 words) | keys n | hist kBuckets | scan sums | perm n | cell tiles
+  return 4ull * (16 + n + kBuckets + (kBuckets / 1024 + 2) + n + cell_words(n));
 }
 
 cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, const uint32_t *d_n, void *scratch, uint32_t **perm_out,
-                           cudaStream_t st) {
+                           cudaStream_t st, RayCells *cells) {
   uint32_t *ext = static_cast<uint32_t *>(scratch);
   uint32_t *keys = ext + 16;
   uint32_t *hist = keys + n;
@@ -167,6 +208,16 @@ cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, const uint32_t *d_n, 
   e = exclusive_scan_u32(hist, hist, sums, kBuckets, st);
   if (e != cudaSuccess) return e;
   k_scatter<<<(n + 255) / 256, 256, 0, st>>>(keys, n, d_n, hist, perm);
+  if (!cells) return cudaGetLastError();
+  uint32_t *cnt = perm + n, *off = cnt + kCells, *csums = off + kCells, *count = csums + (kCells / 1024 + 2);
+  uint32_t *tiles = count + 1;
+  k_cell_count<<<kCells / 256, 256, 0, st>>>(hist, cnt);
+  e = exclusive_scan_u32(cnt, off, csums, kCells, st);
+  if (e != cudaSuccess) return e;
+  k_cell_emit<<<kCells / 256, 256, 0, st>>>(hist, cnt, off, tiles, count);
+  cells->ext = ext;
+  cells->tiles = tiles;
+  cells->count = count;
   return cudaGetLastError();
 }
 

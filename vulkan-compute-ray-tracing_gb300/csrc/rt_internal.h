@@ -84,6 +84,7 @@ struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
   int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
+  int beam = 0;     // 1: sorted one-origin batches traverse the sort's cell tiles as beams (beam.cuh)
   int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
   int packet_minblocks = 12;  // the same for the packet caster
@@ -112,9 +113,13 @@ inline int trace_stack_entries(const TraceOpts &o, const DevScene &sc) {
 // at their ray's input index.
 // chunk_scratch holds trace_chunk_scratch_bytes(n) (the packet pass's list of
 // chunks left for the per-lane pass); without it packets are not used.
+// `cells` (with perm, from the same sort) lets one-origin batches be cast
+// as beams over the sort's cell tiles (trace.beam).
+struct RayCells;
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
                          uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st,
-                         const uint32_t *perm = nullptr, uint32_t *chunk_scratch = nullptr);
+                         const uint32_t *perm = nullptr, uint32_t *chunk_scratch = nullptr,
+                         const RayCells *cells = nullptr);
 size_t trace_chunk_scratch_bytes(uint32_t n);
 // The 8-wide caster over listed 32-ray chunks of a device-sized queue
 // (*d_n rays, at most cap), writing (leaf k, t) hits; wide_ok tells whether
@@ -129,9 +134,21 @@ cudaError_t launch_wide_leaf(const DevScene &sc, const rt_ray *rays, uint32_t ca
 // Morton bucketing of a ray batch (raysort.cu); `scratch` holds
 // raysort_scratch_bytes(n); *perm_out points into it.
 size_t raysort_scratch_bytes(uint32_t n);
-// With d_n != NULL only the first *d_n of the n rays are sorted.
+// The sorted batch cut at cells of 64 Morton buckets (8 x 8 direction
+// buckets when the batch has one origin), each cell into tiles of at most
+// 256 rays: tiles[2t], tiles[2t + 1] = first and one-past-last sorted
+// position of tile t, t < *count. ext[0..4] / ext[5..9]: ordered minima /
+// maxima of the key coordinates (origin x, y, z, octahedral u, v) over the
+// sampled rays. All device pointers into the sort's scratch.
+struct RayCells {
+  const uint32_t *ext = nullptr;
+  const uint32_t *tiles = nullptr;
+  const uint32_t *count = nullptr;
+};
+// With d_n != NULL only the first *d_n of the n rays are sorted. With
+// `cells`, the cell tiles are listed too (not with d_n).
 cudaError_t launch_raysort(const rt_ray *rays, uint32_t n, const uint32_t *d_n, void *scratch, uint32_t **perm_out,
-                           cudaStream_t st);
+                           cudaStream_t st, RayCells *cells = nullptr);
 // The shader-literal 16-entry-stack traversal over the Bvh.h node array.
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
                                    cudaStream_t st);

@@ -19,6 +19,7 @@
 
 #include "rt_internal.h"
 #include "shade.cuh"
+#include "beam.cuh"
 #include "traverse.cuh"
 #include "wide.cuh"
 
@@ -190,10 +191,42 @@ __device__ __forceinline__ void store_hit(const DevScene &sc, int4 *__restrict__
   hits[i] = h;
 }
 
+// One whole-warp chunk: 32 consecutive rays from `base` (in the cast
+// order). If they are coherent (warp_is_coherent) the warp traces them as
+// one packet, otherwise it lists the chunk for k_trace_lanes (or, without a
+// list, traces it per lane in place). Warp-converged call.
+template <int STACK>
+__device__ __forceinline__ void cast_chunk(const DevScene &sc, const float4 *__restrict__ rays, uint32_t n,
+                                           int4 *__restrict__ hits, uint32_t *err, const uint32_t *__restrict__ perm,
+                                           uint32_t *__restrict__ list, uint32_t *__restrict__ list_count,
+                                           bool refine, uint32_t base, uint32_t lane, int *s_stack) {
+  uint32_t i = base + lane;
+  const bool active = i < n;
+  f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
+  float tmin = 0.0f, tmax = 0.0f;
+  if (active) {
+    if (perm) i = __ldg(perm + i);
+    load_ray(rays, i, o, d, tmin, tmax);
+  }
+  TraceRay r = make_ray(o, d, tmin);
+  float closest = tmax, u = 0.0f, v = 0.0f;
+  int k;
+  if (warp_is_coherent(active, r)) {
+    const int oct = warp_octant(active, r);
+#define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, u, v, s_stack, err)
+    RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+  } else if (list) {
+    if (lane == 0) list[atomicAdd(list_count, 1u)] = base;
+    return;
+  } else {
+    k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
+  }
+  if (active) store_hit(sc, hits, i, k, o, d, closest, u, v, refine);
+}
+
 // First kernel of a whole-warp cast: each warp takes 32 consecutive rays (in
-// the cast order); if they are coherent (warp_is_coherent) the warp traces
-// them as one packet, otherwise it lists the chunk for k_trace_lanes (or,
-// without a list, traces it per lane in place). The postponed-leaf traversal
+// the cast order) at a time (cast_chunk). The postponed-leaf traversal
 // lives in the other kernel: compiled into this one it cost the packet path
 // 8% (measured), while the in-place per-lane path costs nothing.
 template <int STACK, int MINB>
@@ -211,29 +244,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_packets(DevScene sc, const
     if (lane == 0) base = atomicAdd(counter, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) return;
-    uint32_t i = base + lane;
-    const bool active = i < n;
-    f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
-    float tmin = 0.0f, tmax = 0.0f;
-    if (active) {
-      if (perm) i = __ldg(perm + i);
-      load_ray(rays, i, o, d, tmin, tmax);
-    }
-    TraceRay r = make_ray(o, d, tmin);
-    float closest = tmax, u = 0.0f, v = 0.0f;
-    int k;
-    if (warp_is_coherent(active, r)) {
-      const int oct = warp_octant(active, r);
-#define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, u, v, s_stack, err)
-      RTGB_OCT_DISPATCH(oct, RTGB_CALL)
-#undef RTGB_CALL
-    } else if (list) {
-      if (lane == 0) list[atomicAdd(list_count, 1u)] = base;
-      continue;
-    } else {
-      k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
-    }
-    if (active) store_hit(sc, hits, i, k, o, d, closest, u, v, refine);
+    cast_chunk<STACK>(sc, rays, n, hits, err, perm, list, list_count, refine, base, lane, s_stack);
   }
 }
 
@@ -276,6 +287,199 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_lanes(DevScene sc, const f
       k = active ? traverse_closest<STACK>(sc, r, closest, u, v, err) : -1;
     }
     if (active) store_hit(sc, hits, i, k, o, d, closest, u, v, refine);
+  }
+}
+
+// Beam cast (beam.cuh). With the ray sort's cell tiles and a batch of one
+// origin (the sort's sampled origin extent is zero), each block casts one
+// cell tile at a time: up to 256 rays in 8 warps plus a producer warp. A
+// tile whose rays share the origin and whose directions fit a narrow cone
+// around one axis walks the tree once as a beam, in rounds: the producer
+// fills the next round while the ray warps test the current one, with one
+// block barrier per round. Any other tile, or one whose beam was
+// abandoned, is cast warp by warp in place (packet, or per lane). Other
+// batches are cast in 32-ray chunks by all warps, as k_trace_packets
+// casts them.
+template <int STACK, int MINB>
+__global__ void __launch_bounds__(kBeamThreads, MINB)
+    k_trace_beams(DevScene sc, const float4 *__restrict__ rays, uint32_t n, int4 *__restrict__ hits,
+                  uint32_t *__restrict__ counter, uint32_t *err, const uint32_t *__restrict__ perm,
+                  uint32_t *__restrict__ list, uint32_t *__restrict__ list_count,
+                  const uint32_t *__restrict__ cell_tiles, const uint32_t *__restrict__ cell_count,
+                  const uint32_t *__restrict__ ext, bool refine) {
+  __shared__ BeamShared s;
+  extern __shared__ int s_dyn_stack[];  // STACK entries per warp (packet casts)
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int *const s_stack = s_dyn_stack + warp * STACK;
+  const float INF = __int_as_float(0x7f800000);
+  const bool one_origin = __ldg(ext + 0) == __ldg(ext + 5) && __ldg(ext + 1) == __ldg(ext + 6) &&
+                          __ldg(ext + 2) == __ldg(ext + 7);
+  if (!one_origin) {
+    for (;;) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(counter, 32u);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= n) return;
+      cast_chunk<STACK>(sc, rays, n, hits, err, perm, list, list_count, refine, base, lane, s_stack);
+    }
+  }
+  const uint32_t ntiles = __ldg(cell_count);
+  const bool producer = warp == kBeamRayWarps;
+  for (;;) {
+    __syncthreads();  // every thread is done with the previous tile's state
+    if (tid == 0) s.tile = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t t = s.tile;
+    if (t >= ntiles) return;
+    const uint32_t beg = __ldg(cell_tiles + 2 * t), end = __ldg(cell_tiles + 2 * t + 1);
+    uint32_t i = beg + tid;
+    const bool active = !producer && i < end && i < n;
+    f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
+    float tmin = 0.0f, tmax = 0.0f;
+    if (active) {
+      i = __ldg(perm + i);
+      load_ray(rays, i, o, d, tmin, tmax);
+    }
+    const TraceRay r = make_ray(o, d, tmin);
+    // The tile's origin, dominant axis and near-first octant from its
+    // first ray (thread 0's: every tile holds at least one ray).
+    if (tid == 0) {
+      s.o[0] = o.x, s.o[1] = o.y, s.o[2] = o.z;
+      const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+      const int za = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+      s.za = za;
+      s.sz = (za == 0 ? d.x : (za == 1 ? d.y : d.z)) >= 0.0f ? 1.0f : -1.0f;
+      s.oct = ray_octant(r);
+      s.u_lo = s.v_lo = 0xffffffffu;
+      s.u_hi = s.v_hi = 0u;
+      s.md[0] = 0u;
+      s.md[1] = 0x7f800000u;
+      s.sp = 0;
+    }
+    __syncthreads();
+    // Every ray: the same origin, in front along the tile's axis within
+    // 2:1 of it, and (u, v) = (d_u, d_v) / d_z folded into the tile's and
+    // the warp's bounds.
+    bool ok = true;
+    uint32_t ulo = 0xffffffffu, uhi = 0u, vlo = 0xffffffffu, vhi = 0u;
+    const int za = s.za;
+    const float sz = s.sz;
+    if (active) {
+      const float dz = sz * (za == 0 ? d.x : (za == 1 ? d.y : d.z));
+      const float du = za == 0 ? d.y : (za == 1 ? d.z : d.x);
+      const float dv = za == 0 ? d.z : (za == 1 ? d.x : d.y);
+      ok = o.x == s.o[0] && o.y == s.o[1] && o.z == s.o[2] && dz > 0.0f && fabsf(du) <= 2.0f * dz &&
+           fabsf(dv) <= 2.0f * dz;
+      if (ok) {
+        ulo = uhi = beam_ord(__fdiv_rn(du, dz));
+        vlo = vhi = beam_ord(__fdiv_rn(dv, dz));
+      }
+    }
+    ulo = __reduce_min_sync(0xffffffffu, ulo);
+    uhi = __reduce_max_sync(0xffffffffu, uhi);
+    vlo = __reduce_min_sync(0xffffffffu, vlo);
+    vhi = __reduce_max_sync(0xffffffffu, vhi);
+    if (lane == 0 && !producer) {
+      atomicMin(&s.u_lo, ulo);
+      atomicMax(&s.u_hi, uhi);
+      atomicMin(&s.v_lo, vlo);
+      atomicMax(&s.v_hi, vhi);
+    }
+    ok = __syncthreads_and(ok);
+    if (tid == 0) {
+      // Bounds widened by 1e-5 (the quotients carry one rounding).
+      const float umin = beam_unord(s.u_lo) - 1e-5f, umax = beam_unord(s.u_hi) + 1e-5f;
+      const float vmin = beam_unord(s.v_lo) - 1e-5f, vmax = beam_unord(s.v_hi) + 1e-5f;
+      s.lim[0] = umin, s.lim[1] = umax, s.lim[2] = vmin, s.lim[3] = vmax;
+      // A one-triangle tree (the root a leaf) goes to the packets.
+      s.ok = ok && sc.root_ref >= 0 && umax - umin <= kBeamMaxSpan && vmax - vmin <= kBeamMaxSpan;
+      if (s.ok) {
+        s.stack[0] = sc.root_ref;
+        s.sp = 1;
+      }
+    }
+    __syncthreads();
+    float closest = tmax, bu = 0.0f, bv = 0.0f;
+    int best = -1;
+    bool beam = s.ok != 0;
+    if (beam) {
+      Cone tcone;
+      tcone.o[0] = s.o[0], tcone.o[1] = s.o[1], tcone.o[2] = s.o[2];
+      tcone.umin = s.lim[0], tcone.umax = s.lim[1], tcone.vmin = s.lim[2], tcone.vmax = s.lim[3];
+      tcone.sz = sz;
+      tcone.za = za;
+      // The warp's own cone (empty, inverted bounds, for a warp without rays).
+      Cone wcone = tcone;
+      wcone.umin = beam_unord(ulo) - 1e-5f, wcone.umax = beam_unord(uhi) + 1e-5f;
+      wcone.vmin = beam_unord(vlo) - 1e-5f, wcone.vmax = beam_unord(vhi) + 1e-5f;
+      const int woct = warp_octant(active, r);
+      const float dn = active ? __fsqrt_rn(dot3(d, d)) : 0.0f;
+#define RTGB_EXPAND(BUF, MD2)                                                    \
+  (za == 0 ? beam_expand<0, kBeamPop>(s, tcone, sc, lane, err, BUF, MD2)           \
+   : za == 1 ? beam_expand<1, kBeamPop>(s, tcone, sc, lane, err, BUF, MD2)         \
+             : beam_expand<2, kBeamPop>(s, tcone, sc, lane, err, BUF, MD2))
+      if (producer) RTGB_EXPAND(0, INF);
+      __syncthreads();
+      for (int k = 0;; k++) {
+        const int cur = k & 1;
+        const int nl = s.nleaf[cur], rs = s.rstate[cur];
+        if (rs == kRoundAbandon) {
+          beam = false;
+          break;
+        }
+        if (producer) {
+          if (rs == kRoundMore) {
+            // Depth bound: the farthest closest hit after the previous round.
+            const float md = __uint_as_float(s.md[cur ^ 1]);
+            __syncwarp();
+            if (lane == 0) s.md[cur ^ 1] = 0u;
+            RTGB_EXPAND(cur ^ 1, md * md);
+          }
+        } else {
+          // Farthest closest hit of the warp's rays, as a distance (unknown
+          // values count as infinite). The 1% margin exceeds the fp32
+          // triangle t's own error except at grazing angles below ~1e-5
+          // rad, where a hit's t may undershoot its distance.
+          uint32_t wm = 0u;
+          if (active) {
+            const float x = closest * dn * 1.01f;
+            wm = x >= 0.0f ? __float_as_uint(x) : (x < 0.0f ? 0u : 0x7f800000u);
+          }
+          const float wmd = __uint_as_float(__reduce_max_sync(0xffffffffu, wm));
+#define RTGB_CALL(O) beam_test_round<O>(s, cur, nl, wcone, wmd * wmd, lane, sc, r, active, closest, best, bu, bv)
+          RTGB_OCT_DISPATCH(woct, RTGB_CALL)
+#undef RTGB_CALL
+          wm = 0u;
+          if (active) {
+            const float x = closest * dn * 1.01f;
+            wm = x >= 0.0f ? __float_as_uint(x) : (x < 0.0f ? 0u : 0x7f800000u);
+          }
+          wm = __reduce_max_sync(0xffffffffu, wm);
+          if (lane == 0) atomicMax(&s.md[cur], wm);
+        }
+        __syncthreads();
+        if (rs != kRoundMore) break;
+      }
+#undef RTGB_EXPAND
+    }
+    if (producer) continue;
+    if (beam) {
+      if (active) store_hit(sc, hits, i, best, o, d, closest, bu, bv, refine);
+      continue;
+    }
+    // Warp by warp, in place, from the start.
+    closest = tmax;
+    bu = bv = 0.0f;
+    int k;
+    if (warp_is_coherent(active, r)) {
+      const int oct = warp_octant(active, r);
+#define RTGB_CALL(O) k = traverse_packet<STACK, O>(sc, r, active, closest, bu, bv, s_stack, err)
+      RTGB_OCT_DISPATCH(oct, RTGB_CALL)
+#undef RTGB_CALL
+    } else {
+      k = active ? traverse_closest<STACK>(sc, r, closest, bu, bv, err) : -1;
+    }
+    if (active) store_hit(sc, hits, i, k, o, d, closest, bu, bv, refine);
   }
 }
 
@@ -675,7 +879,7 @@ cudaError_t launch_wide_any(const DevScene &sc, const float4 *rays, uint32_t n, 
 template <int STACK>
 cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
                            uint32_t *err, const TraceOpts &opts, const uint32_t *perm, uint32_t *chunk_scratch,
-                           bool refine, cudaStream_t st) {
+                           const RayCells *cells, bool refine, cudaStream_t st) {
   const float4 *r4 = reinterpret_cast<const float4 *>(rays);
   int4 *h4 = reinterpret_cast<int4 *>(hits);
   if (opts.refill >= 32) {
@@ -686,12 +890,20 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
     if (opts.packet && chunk_scratch) {
       cudaError_t e = cudaMemsetAsync(chunk_scratch, 0, 256, st);
       if (e != cudaSuccess) return e;
-      auto pk = opts.packet_minblocks >= 16   ? k_trace_packets<STACK, 16>
-                : opts.packet_minblocks >= 12 ? k_trace_packets<STACK, 12>
-                                              : k_trace_packets<STACK, 10>;
-      const size_t smem = (size_t)(block / 32) * STACK * sizeof(int);
-      pk<<<persistent_grid(pk, n, block, smem), block, smem, st>>>(
-          sc, r4, n, h4, counter, err, perm, opts.defer ? chunk_scratch + 64 : nullptr, chunk_scratch, refine);
+      uint32_t *plist = opts.defer ? chunk_scratch + 64 : nullptr;
+      if (opts.beam && cells && perm) {
+        auto bk = k_trace_beams<STACK, 3>;
+        const size_t smem = (size_t)(kBeamThreads / 32) * STACK * sizeof(int);
+        bk<<<persistent_grid(bk, n, kBeamThreads, smem), kBeamThreads, smem, st>>>(
+            sc, r4, n, h4, counter, err, perm, plist, chunk_scratch, cells->tiles, cells->count, cells->ext, refine);
+      } else {
+        auto pk = opts.packet_minblocks >= 16   ? k_trace_packets<STACK, 16>
+                  : opts.packet_minblocks >= 12 ? k_trace_packets<STACK, 12>
+                                                : k_trace_packets<STACK, 10>;
+        const size_t smem = (size_t)(block / 32) * STACK * sizeof(int);
+        pk<<<persistent_grid(pk, n, block, smem), block, smem, st>>>(sc, r4, n, h4, counter, err, perm, plist,
+                                                                     chunk_scratch, refine);
+      }
       if (!opts.defer) return cudaGetLastError();
       list = chunk_scratch + 64;
       list_count = chunk_scratch;
@@ -751,7 +963,7 @@ size_t trace_chunk_scratch_bytes(uint32_t n) { return 4ull * (64 + (n + 31) / 32
 
 cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits, uint32_t *counter,
                          uint32_t *err, bool refine, const TraceOpts &opts, cudaStream_t st, const uint32_t *perm,
-                         uint32_t *chunk_scratch) {
+                         uint32_t *chunk_scratch, const RayCells *cells) {
   if (n == 0) return cudaSuccess;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -764,9 +976,10 @@ cudaError_t launch_trace(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_
   // Traversal stack: trace.stack entries (16, 32 or 64), raised to the
   // smallest size that holds the tree's depth.
   const int stk = trace_stack_entries(opts, sc);
-  return stk <= 16   ? launch_variant<16>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, refine, st)
-         : stk <= 32 ? launch_variant<32>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, refine, st)
-                     : launch_variant<64>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, refine, st);
+  return stk <= 16 ? launch_variant<16>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, cells, refine, st)
+         : stk <= 32
+             ? launch_variant<32>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, cells, refine, st)
+             : launch_variant<64>(sc, rays, n, hits, counter, err, opts, perm, chunk_scratch, cells, refine, st);
 }
 
 cudaError_t launch_trace_literal16(const DevScene &sc, const rt_ray *rays, uint32_t n, rt_hit *hits,
