@@ -176,11 +176,12 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   traversal per lane. Results are identical either way
  *   "trace.beam"    1 = sorted batches of one origin are cast in tiles of up
  *                   to 256 rays (the sort's Morton cells) that walk the tree
- *                   once as a beam: one warp expands the tile's cone, the
+ *                   once as a beam: the block expands the tile's cone, the
  *                   rays test the leaves it meets (each with its own slab
- *                   test first); 0 (default) = warp packets. Results are
- *                   identical either way; beams pay off on trees whose boxes
- *                   overlap heavily (the reference's), packets on tight ones
+ *                   test first); 0 = warp packets; 2 (default) = beams on
+ *                   Bvh.h's median-split tree (bvh.builder 0 or the caller's
+ *                   nodes), whose overlapping boxes favour them, packets on
+ *                   the LBVH and PLOC trees. Results are identical either way
  *   "trace.spec"    1 (default) = per-lane traversal parks the first leaf it
  *                   reaches and keeps descending until every lane of the
  *                   warp holds one, then tests them together; 0 = test each

@@ -420,6 +420,7 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   if (nl) UCK(cudaMemcpyAsync(slab + off_lights, lights, sizeof(rt_light) * nl, cudaMemcpyHostToDevice, st), "upload lights");
   if (ns) UCK(cudaMemcpyAsync(slab + off_spheres, spheres, sizeof(rt_sphere) * ns, cudaMemcpyHostToDevice, st), "upload spheres");
   rt_bvh_node *dnodes = (rt_bvh_node *)(slab + off_nodes);
+  bool median_tree = nodes != nullptr;
   if (nodes) {
     UCK(cudaMemcpyAsync(dnodes, nodes, sizeof(rt_bvh_node) * nnodes, cudaMemcpyHostToDevice, st), "upload nodes");
   } else {
@@ -439,6 +440,7 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
       bs = gpu_build_ploc((const rt_triangle *)(slab + off_tris), nt, (uint32_t)ploc_radius, dnodes, st,
                           &sc->build_ms, &depth, errbuf, sizeof(errbuf));
     } else {
+      median_tree = true;
       std::vector<uint8_t> axes(nnodes);
       glibc_rand_axes(bvh_seed, nnodes, axes.data());
       bs = gpu_build_bvh((const rt_triangle *)(slab + off_tris), nt, axes.data(), dnodes, st, &sc->build_ms, &depth,
@@ -448,6 +450,7 @@ rt_status rtUploadScene(rt_ctx *ctx, const rt_triangle *tris, uint32_t nt, const
   }
   d.depth = depth;
   if (depth > 64) return abort_upload(fail(ctx, RT_ERR_INVALID_SCENE, "tree depth %u exceeds 64", depth));
+  d.median_tree = median_tree ? 1u : 0u;
   // Traversal layout.
   {
     uint32_t *scratch = nullptr;
@@ -788,7 +791,7 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     return RT_SUCCESS;
   }
   if (k == "trace.beam") {
-    if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
+    if (value < 0 || value > 2) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.beam = (int)value;
     return RT_SUCCESS;
   }

@@ -3,14 +3,15 @@
 // warp packet. The beam is the cone of directions over the tile's rays,
 // bounded by four planes through the origin in the projection on the rays'
 // dominant axis (u = d_u / d_z, v = d_v / d_z over the tile), plus the
-// half-space in front of the origin. A producer warp expands the beam's
-// frontier, up to 32 stacked nodes at a time (one per lane, nearest first),
-// and collects the leaves whose boxes meet the beam into rounds of at least
-// 64; while it fills the next round, the eight ray warps test the current
-// one: each warp first drops the leaves outside its own, narrower cone (one
-// leaf per lane), then every lane runs its own slab test on each remaining
-// leaf and the triangle test where that passes (traverse.cuh:
-// slab_hit_child, test_triangle).
+// half-space in front of the origin. The block alternates two phases.
+// Expansion: all eight warps pop up to 256 frontier nodes at once (one per
+// thread, nearest first), test both children of each against the tile's
+// cone, append the leaves to the round and push the inner children back
+// in order; steps repeat until the round holds 64 leaves or the frontier is
+// empty. Testing: each warp drops the round's leaves outside its own,
+// narrower cone (one leaf per lane), then every lane runs its own slab test
+// on each remaining leaf and the triangle test where that passes
+// (traverse.cuh: slab_hit_child, test_triangle).
 //
 // Results equal the per-ray traversal's. A ray's slab test passes a box
 // only if the ray meets the box (to within the rounding of the slab
@@ -29,32 +30,26 @@
 
 namespace rtgb {
 
-constexpr int kBeamRayWarps = 8;                       // warps holding rays
-constexpr int kBeamRays = 32 * kBeamRayWarps;          // rays per tile, one per thread
-constexpr int kBeamThreads = kBeamRays + 32;           // plus the producer warp
-constexpr int kBeamStack = 2048;                       // frontier entries (inner node refs)
-constexpr int kBeamBatch = 64;                         // leaves per round (at least, but the last)
-constexpr int kBeamPop = 1;                            // frontier entries per producer lane and step
-constexpr int kBeamLeafCap = kBeamBatch + 64 * kBeamPop;  // one step adds at most 64 per entry a lane pops
+constexpr int kBeamWarps = 8;
+constexpr int kBeamRays = 32 * kBeamWarps;            // rays per tile, one per thread
+constexpr int kBeamStack = 2048;                      // frontier entries (inner node refs)
+constexpr int kBeamBatch = 64;                        // leaves per round (at least, but the last)
+constexpr int kBeamLeafCap = kBeamBatch + 2 * kBeamRays;  // one step adds at most two per thread
 // Largest extent of a tile's directions in the projection (u and v each);
 // wider tiles go to the warp packets.
 constexpr float kBeamMaxSpan = 0.25f;
 
-// Round states (rstate): the last round, more rounds follow, abandoned.
-constexpr int kRoundLast = 0, kRoundMore = 1, kRoundAbandon = 2;
-
 struct BeamShared {
-  float4 leaf[2][kBeamLeafCap][2];  // two rounds of child records (traverse.cuh layout)
+  float4 leaf[kBeamLeafCap][2];  // the round's child records (traverse.cuh layout)
   int stack[kBeamStack];
+  int2 cnt[kBeamWarps];  // per warp and step: pushes, leaves
   float o[3];       // the tile's origin
   float lim[4];     // umin, umax, vmin, vmax of the tile's cone (widened)
   float sz;         // sign of the dominant axis
   uint32_t u_lo, u_hi, v_lo, v_hi;  // ordered-float reductions of u and v
-  uint32_t md[2];   // per round: farthest closest-hit distance after its tests (fp32 bits, >= 0)
+  uint32_t md[2];   // per round (alternating): farthest closest-hit distance after its tests (fp32 bits)
   uint32_t tile;    // the tile being cast
   int za, oct, ok;  // dominant axis, near-first octant, beam usable
-  int sp;           // frontier size (producer only)
-  int nleaf[2], rstate[2];
 };
 
 // fp32 to uint32 with unsigned order equal to float order (for min/max).
@@ -103,113 +98,91 @@ __device__ __forceinline__ bool cone_box(const Cone &c, float4 p, float4 q, floa
   return in && (du * du + dv * dv + dz * dz <= maxd2);
 }
 
-// The producer warp (all 32 lanes, converged) fills round buffer `buf`:
-// it expands the frontier until the round holds kBeamBatch leaves or the
-// frontier is empty. Each step pops up to 32 * E entries (entry j in lane
-// j % 32, the top first), tests both children of each popped node against
-// the tile's cone (the E node loads of a lane in flight together), appends
-// the leaves to the round and pushes the inner children back with the
-// popped order kept (entry 0's near child on top). A frontier overflow, a
-// bad ref or more steps than the tree has nodes abandon the beam: the tile
-// is then cast by warp packets.
-template <int ZA, int E>
-__device__ __forceinline__ void beam_expand(BeamShared &s, const Cone &cone, const DevScene &sc, uint32_t lane,
-                                            uint32_t *err, int buf, float maxd2) {
+// One expansion step by the whole block (block-converged call with two
+// block barriers; sp and nleaf are the same in every thread). Thread j
+// pops frontier entry j from the top, tests both children of its node
+// against the tile's cone, and the block appends the leaves to the round
+// and pushes the inner children back with the popped order kept: deeper
+// entries' children below, entry 0's near child on top. Returns false,
+// with nothing written, on a bad ref (reported) or when the frontier or the
+// round would overflow.
+template <int ZA>
+__device__ __forceinline__ bool beam_step(BeamShared &s, const Cone &cone, const DevScene &sc, uint32_t lane,
+                                          uint32_t warp, int &sp, int &nleaf, float maxd2, uint32_t *err) {
   const uint32_t lt = (1u << lane) - 1u, gt = ~lt & ~(1u << lane);
-  int sp = s.sp, nleaf = 0, state = kRoundMore;
-  const float4 *__restrict__ bvh = sc.bvh2;
-  const uint32_t inner_count = sc.ntris - 1u;  // pair nodes
-  uint32_t steps = 0;
-  while (sp > 0 && nleaf < kBeamBatch) {
-    const int take = sp < 32 * E ? sp : 32 * E;
-    int node[E];
-    bool mine[E], bad = false;
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-      mine[e] = (int)lane + 32 * e < take;
-      node[e] = mine[e] ? s.stack[sp - 1 - (int)lane - 32 * e] : 0;
-      bad |= mine[e] && (uint32_t)node[e] >= inner_count;
-    }
-    sp -= take;
-    bad = __any_sync(0xffffffffu, bad);
-    if (bad || ++steps > sc.ntris + 16u) {
-      if (lane == 0) atomicOr(err, bad ? KERR_BAD_INDEX : KERR_TIMEOUT);
-      state = kRoundAbandon;
-      break;
-    }
-    float4 a[E], b[E], c[E], d[E];
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-      a[e] = b[e] = c[e] = d[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (mine[e]) load_node(bvh + 4ll * node[e], a[e], b[e], c[e], d[e]);
-    }
-    // Deeper popped entries (higher j) first: their children go below.
-    bool full = false;
-#pragma unroll
-    for (int e = E - 1; e >= 0; e--) {
-      const bool h0 = mine[e] && cone_box<ZA>(cone, a[e], b[e], maxd2);
-      const bool h1 = mine[e] && cone_box<ZA>(cone, c[e], d[e], maxd2);
-      const int r0 = __float_as_int(b[e].z), r1 = __float_as_int(d[e].z);
-      const bool in0 = h0 && r0 >= 0, in1 = h1 && r1 >= 0, lf0 = h0 && r0 < 0, lf1 = h1 && r1 < 0;
-      const uint32_t bi0 = __ballot_sync(0xffffffffu, in0), bi1 = __ballot_sync(0xffffffffu, in1);
-      const uint32_t bl0 = __ballot_sync(0xffffffffu, lf0), bl1 = __ballot_sync(0xffffffffu, lf1);
-      const int pushes = __popc(bi0) + __popc(bi1), leaves = __popc(bl0) + __popc(bl1);
-      if (sp + pushes > kBeamStack || nleaf + leaves > kBeamLeafCap) {
-        full = true;
-        break;
-      }
-      const int pos = sp + __popc(bi0 & gt) + __popc(bi1 & gt);
-      if (in0 && in1) {
-        const bool f1 = child1_first(b[e], s.oct);
-        s.stack[pos] = f1 ? r0 : r1;      // far
-        s.stack[pos + 1] = f1 ? r1 : r0;  // near, on top
-      } else if (in0 || in1) {
-        s.stack[pos] = in0 ? r0 : r1;
-      }
-      sp += pushes;
-      int lpos = nleaf + __popc(bl0 & lt) + __popc(bl1 & lt);
-      if (lf0) {
-        s.leaf[buf][lpos][0] = a[e];
-        s.leaf[buf][lpos][1] = b[e];
-        lpos++;
-      }
-      if (lf1) {
-        s.leaf[buf][lpos][0] = c[e];
-        s.leaf[buf][lpos][1] = d[e];
-      }
-      nleaf += leaves;
-    }
-    if (full) {
-      state = kRoundAbandon;
-      break;
-    }
-    __syncwarp();
+  const int j = (int)(warp * 32u + lane);
+  const int take = sp < kBeamRays ? sp : kBeamRays;
+  const bool mine = j < take;
+  const int node = mine ? s.stack[sp - 1 - j] : 0;
+  const bool bad = mine && (uint32_t)node >= sc.ntris - 1u;  // pair nodes are 0 .. ntris - 2
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a, c = a, d = a;
+  bool h0 = false, h1 = false;
+  if (mine && !bad) {
+    load_node(sc.bvh2 + 4ll * node, a, b, c, d);
+    h0 = cone_box<ZA>(cone, a, b, maxd2);
+    h1 = cone_box<ZA>(cone, c, d, maxd2);
   }
-  if (state == kRoundMore && sp == 0) state = kRoundLast;
-  __syncwarp();
-  if (lane == 0) {
-    s.sp = sp;
-    s.nleaf[buf] = nleaf;
-    s.rstate[buf] = state;
+  const int r0 = __float_as_int(b.z), r1 = __float_as_int(d.z);
+  const bool in0 = h0 && r0 >= 0, in1 = h1 && r1 >= 0, lf0 = h0 && r0 < 0, lf1 = h1 && r1 < 0;
+  const uint32_t bi0 = __ballot_sync(0xffffffffu, in0), bi1 = __ballot_sync(0xffffffffu, in1);
+  const uint32_t bl0 = __ballot_sync(0xffffffffu, lf0), bl1 = __ballot_sync(0xffffffffu, lf1);
+  if (lane == 0) s.cnt[warp] = make_int2(__popc(bi0) + __popc(bi1), __popc(bl0) + __popc(bl1));
+  if (__syncthreads_or(bad)) {
+    if (warp == 0 && lane == 0) atomicOr(err, KERR_BAD_INDEX);
+    return false;
   }
+  // Deeper warps' children go below; leaves in warp order.
+  int below = sp - take, lbase = nleaf, pushes = 0, leaves = 0;
+#pragma unroll
+  for (int w = 0; w < kBeamWarps; w++) {
+    const int2 cw = s.cnt[w];
+    pushes += cw.x;
+    leaves += cw.y;
+    if (w > (int)warp) below += cw.x;
+    if (w < (int)warp) lbase += cw.y;
+  }
+  const int nsp = sp - take + pushes, nnl = nleaf + leaves;
+  if (nsp > kBeamStack || nnl > kBeamLeafCap) return false;
+  const int pos = below + __popc(bi0 & gt) + __popc(bi1 & gt);
+  if (in0 && in1) {
+    const bool f1 = child1_first(b, s.oct);
+    s.stack[pos] = f1 ? r0 : r1;      // far
+    s.stack[pos + 1] = f1 ? r1 : r0;  // near, on top
+  } else if (in0 || in1) {
+    s.stack[pos] = in0 ? r0 : r1;
+  }
+  int lpos = lbase + __popc(bl0 & lt) + __popc(bl1 & lt);
+  if (lf0) {
+    s.leaf[lpos][0] = a;
+    s.leaf[lpos][1] = b;
+    lpos++;
+  }
+  if (lf1) {
+    s.leaf[lpos][0] = c;
+    s.leaf[lpos][1] = d;
+  }
+  __syncthreads();
+  sp = nsp;
+  nleaf = nnl;
+  return true;
 }
 
-// A ray warp tests round `buf`: leaves outside the warp's cone (within the
+// A warp tests the round: leaves outside the warp's cone (within the
 // warp's farthest closest hit) are dropped one leaf per lane, then every
 // lane tests the rest against its own ray.
 template <int OCT>
-__device__ __forceinline__ void beam_test_round(const BeamShared &s, int buf, int nleaf, const Cone &wcone,
+__device__ __forceinline__ void beam_test_round(const BeamShared &s, int nleaf, const Cone &wcone,
                                                 float wmaxd2, uint32_t lane, const DevScene &sc,
                                                 const TraceRay &r, bool active, float &closest, int &best,
                                                 float &bu, float &bv) {
   for (int c0 = 0; c0 < nleaf; c0 += 32) {
     const int j = c0 + (int)lane;
-    const bool keep = j < nleaf && cone_box<>(wcone, s.leaf[buf][j][0], s.leaf[buf][j][1], wmaxd2);
+    const bool keep = j < nleaf && cone_box<>(wcone, s.leaf[j][0], s.leaf[j][1], wmaxd2);
     uint32_t m = __ballot_sync(0xffffffffu, keep);
     if (!active) continue;
     for (; m; m &= m - 1u) {
       const int k = c0 + __ffs(m) - 1;
-      const float4 p = s.leaf[buf][k][0], q = s.leaf[buf][k][1];
+      const float4 p = s.leaf[k][0], q = s.leaf[k][1];
       if (slab_hit_child<OCT>(r, p, q, closest))
         test_triangle(sc.tpre, sc.leaf_tri, ~__float_as_int(q.z), r, closest, best, bu, bv);
     }

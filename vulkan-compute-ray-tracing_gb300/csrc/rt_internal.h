@@ -58,6 +58,9 @@ struct DevScene {
   const float4 *bvh8;
   uint32_t n8, levels8;  // bvh8 nodes and levels (0 when absent)
   int32_t root8;         // the bvh8 root node (0)
+  // 1 when the tree is Bvh.h's median-split tree (built here or given by
+  // the caller), whose overlapping boxes favour beams (trace.beam 2).
+  uint32_t median_tree;
 };
 
 // ---------------------------------------------------------------- bvh8.cu
@@ -84,7 +87,8 @@ struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
   int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
-  int beam = 0;     // 1: sorted one-origin batches traverse the sort's cell tiles as beams (beam.cuh)
+  int beam = 2;     // sorted one-origin batches traverse the sort's cell tiles as beams (beam.cuh):
+                    // 1 always, 0 never, 2 on Bvh.h's median-split trees (DevScene::median_tree)
   int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
   int packet_minblocks = 12;  // the same for the packet caster

@@ -292,16 +292,15 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_lanes(DevScene sc, const f
 
 // Beam cast (beam.cuh). With the ray sort's cell tiles and a batch of one
 // origin (the sort's sampled origin extent is zero), each block casts one
-// cell tile at a time: up to 256 rays in 8 warps plus a producer warp. A
-// tile whose rays share the origin and whose directions fit a narrow cone
-// around one axis walks the tree once as a beam, in rounds: the producer
-// fills the next round while the ray warps test the current one, with one
-// block barrier per round. Any other tile, or one whose beam was
-// abandoned, is cast warp by warp in place (packet, or per lane). Other
-// batches are cast in 32-ray chunks by all warps, as k_trace_packets
-// casts them.
+// cell tile at a time, up to 256 rays. A tile whose rays share the origin
+// and whose directions fit a narrow cone around one axis walks the tree
+// once as a beam, in rounds: expansion steps by the whole block until the
+// round holds 64 leaves, then every warp tests them. Any other tile, or one
+// whose beam was abandoned, is cast warp by warp in place (packet, or per
+// lane). Other batches are cast in 32-ray chunks, as k_trace_packets casts
+// them.
 template <int STACK, int MINB>
-__global__ void __launch_bounds__(kBeamThreads, MINB)
+__global__ void __launch_bounds__(kBeamRays, MINB)
     k_trace_beams(DevScene sc, const float4 *__restrict__ rays, uint32_t n, int4 *__restrict__ hits,
                   uint32_t *__restrict__ counter, uint32_t *err, const uint32_t *__restrict__ perm,
                   uint32_t *__restrict__ list, uint32_t *__restrict__ list_count,
@@ -324,7 +323,6 @@ __global__ void __launch_bounds__(kBeamThreads, MINB)
     }
   }
   const uint32_t ntiles = __ldg(cell_count);
-  const bool producer = warp == kBeamRayWarps;
   for (;;) {
     __syncthreads();  // every thread is done with the previous tile's state
     if (tid == 0) s.tile = atomicAdd(counter, 1u);
@@ -333,7 +331,7 @@ __global__ void __launch_bounds__(kBeamThreads, MINB)
     if (t >= ntiles) return;
     const uint32_t beg = __ldg(cell_tiles + 2 * t), end = __ldg(cell_tiles + 2 * t + 1);
     uint32_t i = beg + tid;
-    const bool active = !producer && i < end && i < n;
+    const bool active = i < end && i < n;
     f3 o = mk3(0.0f, 0.0f, 0.0f), d = mk3(1.0f, 0.0f, 0.0f);
     float tmin = 0.0f, tmax = 0.0f;
     if (active) {
@@ -352,9 +350,7 @@ __global__ void __launch_bounds__(kBeamThreads, MINB)
       s.oct = ray_octant(r);
       s.u_lo = s.v_lo = 0xffffffffu;
       s.u_hi = s.v_hi = 0u;
-      s.md[0] = 0u;
-      s.md[1] = 0x7f800000u;
-      s.sp = 0;
+      s.md[0] = s.md[1] = 0u;
     }
     __syncthreads();
     // Every ray: the same origin, in front along the tile's axis within
@@ -379,7 +375,7 @@ __global__ void __launch_bounds__(kBeamThreads, MINB)
     uhi = __reduce_max_sync(0xffffffffu, uhi);
     vlo = __reduce_min_sync(0xffffffffu, vlo);
     vhi = __reduce_max_sync(0xffffffffu, vhi);
-    if (lane == 0 && !producer) {
+    if (lane == 0) {
       atomicMin(&s.u_lo, ulo);
       atomicMax(&s.u_hi, uhi);
       atomicMin(&s.v_lo, vlo);
@@ -393,10 +389,7 @@ __global__ void __launch_bounds__(kBeamThreads, MINB)
       s.lim[0] = umin, s.lim[1] = umax, s.lim[2] = vmin, s.lim[3] = vmax;
       // A one-triangle tree (the root a leaf) goes to the packets.
       s.ok = ok && sc.root_ref >= 0 && umax - umin <= kBeamMaxSpan && vmax - vmin <= kBeamMaxSpan;
-      if (s.ok) {
-        s.stack[0] = sc.root_ref;
-        s.sp = 1;
-      }
+      s.stack[0] = sc.root_ref;
     }
     __syncthreads();
     float closest = tmax, bu = 0.0f, bv = 0.0f;
@@ -414,55 +407,57 @@ __global__ void __launch_bounds__(kBeamThreads, MINB)
       wcone.vmin = beam_unord(vlo) - 1e-5f, wcone.vmax = beam_unord(vhi) + 1e-5f;
       const int woct = warp_octant(active, r);
       const float dn = active ? __fsqrt_rn(dot3(d, d)) : 0.0f;
-#define RTGB_EXPAND(BUF, MD2)                                                    \
-  (za == 0 ? beam_expand<0, kBeamPop>(s, tcone, sc, lane, err, BUF, MD2)           \
-   : za == 1 ? beam_expand<1, kBeamPop>(s, tcone, sc, lane, err, BUF, MD2)         \
-             : beam_expand<2, kBeamPop>(s, tcone, sc, lane, err, BUF, MD2))
-      if (producer) RTGB_EXPAND(0, INF);
-      __syncthreads();
-      for (int k = 0;; k++) {
-        const int cur = k & 1;
-        const int nl = s.nleaf[cur], rs = s.rstate[cur];
-        if (rs == kRoundAbandon) {
-          beam = false;
-          break;
+      // Frontier size, round size, depth bound: the same in every thread.
+      int sp = 1, nl = 0, round = 0;
+      float maxd = INF;
+      uint32_t steps = 0;
+      for (;;) {
+        if (sp > 0 && nl < kBeamBatch) {
+          if (++steps > sc.ntris + 16u) {
+            if (tid == 0) atomicOr(err, KERR_TIMEOUT);
+            beam = false;
+            break;
+          }
+          const float md2 = maxd * maxd;
+          const bool stepped = za == 0   ? beam_step<0>(s, tcone, sc, lane, warp, sp, nl, md2, err)
+                               : za == 1 ? beam_step<1>(s, tcone, sc, lane, warp, sp, nl, md2, err)
+                                         : beam_step<2>(s, tcone, sc, lane, warp, sp, nl, md2, err);
+          if (!stepped) {
+            beam = false;
+            break;
+          }
+          continue;
         }
-        if (producer) {
-          if (rs == kRoundMore) {
-            // Depth bound: the farthest closest hit after the previous round.
-            const float md = __uint_as_float(s.md[cur ^ 1]);
-            __syncwarp();
-            if (lane == 0) s.md[cur ^ 1] = 0u;
-            RTGB_EXPAND(cur ^ 1, md * md);
-          }
-        } else {
-          // Farthest closest hit of the warp's rays, as a distance (unknown
-          // values count as infinite). The 1% margin exceeds the fp32
-          // triangle t's own error except at grazing angles below ~1e-5
-          // rad, where a hit's t may undershoot its distance.
-          uint32_t wm = 0u;
-          if (active) {
-            const float x = closest * dn * 1.01f;
-            wm = x >= 0.0f ? __float_as_uint(x) : (x < 0.0f ? 0u : 0x7f800000u);
-          }
-          const float wmd = __uint_as_float(__reduce_max_sync(0xffffffffu, wm));
-#define RTGB_CALL(O) beam_test_round<O>(s, cur, nl, wcone, wmd * wmd, lane, sc, r, active, closest, best, bu, bv)
-          RTGB_OCT_DISPATCH(woct, RTGB_CALL)
+        if (nl == 0) break;  // frontier and round empty
+        // Farthest closest hit of the warp's rays, as a distance (unknown
+        // values count as infinite). The 1% margin exceeds the fp32
+        // triangle t's own error except at grazing angles below ~1e-5 rad,
+        // where a hit's t may undershoot its distance.
+        uint32_t wm = 0u;
+        if (active) {
+          const float x = closest * dn * 1.01f;
+          wm = x >= 0.0f ? __float_as_uint(x) : (x < 0.0f ? 0u : 0x7f800000u);
+        }
+        const float wmd = __uint_as_float(__reduce_max_sync(0xffffffffu, wm));
+#define RTGB_CALL(O) beam_test_round<O>(s, nl, wcone, wmd * wmd, lane, sc, r, active, closest, best, bu, bv)
+        RTGB_OCT_DISPATCH(woct, RTGB_CALL)
 #undef RTGB_CALL
-          wm = 0u;
-          if (active) {
-            const float x = closest * dn * 1.01f;
-            wm = x >= 0.0f ? __float_as_uint(x) : (x < 0.0f ? 0u : 0x7f800000u);
-          }
-          wm = __reduce_max_sync(0xffffffffu, wm);
-          if (lane == 0) atomicMax(&s.md[cur], wm);
+        wm = 0u;
+        if (active) {
+          const float x = closest * dn * 1.01f;
+          wm = x >= 0.0f ? __float_as_uint(x) : (x < 0.0f ? 0u : 0x7f800000u);
         }
+        wm = __reduce_max_sync(0xffffffffu, wm);
+        // This round's slot collects the maxima; the other one, read after
+        // the previous round, is cleared for the next.
+        if (tid == 0) s.md[(round + 1) & 1] = 0u;
+        if (lane == 0) atomicMax(&s.md[round & 1], wm);
         __syncthreads();
-        if (rs != kRoundMore) break;
+        maxd = __uint_as_float(s.md[round & 1]);
+        round++;
+        nl = 0;
       }
-#undef RTGB_EXPAND
     }
-    if (producer) continue;
     if (beam) {
       if (active) store_hit(sc, hits, i, best, o, d, closest, bu, bv, refine);
       continue;
@@ -891,10 +886,10 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
       cudaError_t e = cudaMemsetAsync(chunk_scratch, 0, 256, st);
       if (e != cudaSuccess) return e;
       uint32_t *plist = opts.defer ? chunk_scratch + 64 : nullptr;
-      if (opts.beam && cells && perm) {
-        auto bk = k_trace_beams<STACK, 3>;
-        const size_t smem = (size_t)(kBeamThreads / 32) * STACK * sizeof(int);
-        bk<<<persistent_grid(bk, n, kBeamThreads, smem), kBeamThreads, smem, st>>>(
+      if ((opts.beam == 1 || (opts.beam == 2 && sc.median_tree)) && cells && perm) {
+        auto bk = k_trace_beams<STACK, 4>;
+        const size_t smem = (size_t)(kBeamRays / 32) * STACK * sizeof(int);
+        bk<<<persistent_grid(bk, n, kBeamRays, smem), kBeamRays, smem, st>>>(
             sc, r4, n, h4, counter, err, perm, plist, chunk_scratch, cells->tiles, cells->count, cells->ext, refine);
       } else {
         auto pk = opts.packet_minblocks >= 16   ? k_trace_packets<STACK, 16>
