@@ -182,6 +182,8 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   Bvh.h's median-split tree (bvh.builder 0 or the caller's
  *                   nodes), whose overlapping boxes favour them, packets on
  *                   the LBVH and PLOC trees. Results are identical either way
+ *   "trace.beam_round"  leaves a beam collects before its rays test them
+ *                   (16..256, default 64)
  *   "trace.spec"    1 (default) = per-lane traversal parks the first leaf it
  *                   reaches and keeps descending until every lane of the
  *                   warp holds one, then tests them together; 0 = test each

@@ -407,6 +407,10 @@ def test_tuning_keys(rt, ctx):
     with pytest.raises(rt.RtError):
         ctx.set_tuning("trace.refill", 0)
     assert 1 <= ctx.get_tuning("trace.refill") <= 32
+    for key, bad in (("trace.beam", 3), ("trace.beam", -1), ("trace.beam_round", 15), ("trace.beam_round", 257)):
+        with pytest.raises(rt.RtError):
+            ctx.set_tuning(key, bad)
+    assert ctx.get_tuning("trace.beam") == 2 and ctx.get_tuning("trace.beam_round") == 64
 
 
 @pytest.mark.parametrize("builder", [1, 2], ids=["lbvh", "ploc"])

@@ -795,6 +795,11 @@ rt_status rtSetTuning(rt_ctx *ctx, const char *key, int64_t value) {
     ctx->trace_opts.beam = (int)value;
     return RT_SUCCESS;
   }
+  if (k == "trace.beam_round") {
+    if (value < 16 || value > 256) return RT_ERR_INVALID_ARGUMENT;
+    ctx->trace_opts.beam_round = (int)value;
+    return RT_SUCCESS;
+  }
   if (k == "trace.spec") {
     if (value < 0 || value > 1) return RT_ERR_INVALID_ARGUMENT;
     ctx->trace_opts.spec = (int)value;
@@ -922,6 +927,10 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value) {
   }
   if (k == "trace.beam") {
     *value = ctx->trace_opts.beam;
+    return RT_SUCCESS;
+  }
+  if (k == "trace.beam_round") {
+    *value = ctx->trace_opts.beam_round;
     return RT_SUCCESS;
   }
   if (k == "trace.spec") {

@@ -7,8 +7,8 @@
 // Expansion: all eight warps pop up to 256 frontier nodes at once (one per
 // thread, nearest first), test both children of each against the tile's
 // cone, append the leaves to the round and push the inner children back
-// in order; steps repeat until the round holds 64 leaves or the frontier is
-// empty. Testing: each warp drops the round's leaves outside its own,
+// in order; steps repeat until the round holds trace.beam_round leaves (64)
+// or the frontier is empty. Testing: each warp drops the round's leaves outside its own,
 // narrower cone (one leaf per lane), then every lane runs its own slab test
 // on each remaining leaf and the triangle test where that passes
 // (traverse.cuh: slab_hit_child, test_triangle).
@@ -33,8 +33,8 @@ namespace rtgb {
 constexpr int kBeamWarps = 8;
 constexpr int kBeamRays = 32 * kBeamWarps;            // rays per tile, one per thread
 constexpr int kBeamStack = 2048;                      // frontier entries (inner node refs)
-constexpr int kBeamBatch = 64;                        // leaves per round (at least, but the last)
-constexpr int kBeamLeafCap = kBeamBatch + 2 * kBeamRays;  // one step adds at most two per thread
+constexpr int kBeamRoundMax = 256;                    // leaves a round collects before testing (trace.beam_round, at most)
+constexpr int kBeamLeafCap = kBeamRoundMax + 2 * kBeamRays;  // one step adds at most two per thread
 // Largest extent of a tile's directions in the projection (u and v each);
 // wider tiles go to the warp packets.
 constexpr float kBeamMaxSpan = 0.25f;

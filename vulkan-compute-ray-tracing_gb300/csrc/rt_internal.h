@@ -89,6 +89,7 @@ struct TraceOpts {
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
   int beam = 2;     // sorted one-origin batches traverse the sort's cell tiles as beams (beam.cuh):
                     // 1 always, 0 never, 2 on Bvh.h's median-split trees (DevScene::median_tree)
+  int beam_round = 64;  // leaves a beam round collects before its rays test them (16..256)
   int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
   int minblocks = 12;  // resident 128-thread blocks per SM the per-lane caster is compiled for (16, 12 or 10)
   int packet_minblocks = 12;  // the same for the packet caster

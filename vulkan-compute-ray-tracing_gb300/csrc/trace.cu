@@ -295,7 +295,7 @@ __global__ void __maxnreg__(regs_for<MINB>()) k_trace_lanes(DevScene sc, const f
 // cell tile at a time, up to 256 rays. A tile whose rays share the origin
 // and whose directions fit a narrow cone around one axis walks the tree
 // once as a beam, in rounds: expansion steps by the whole block until the
-// round holds 64 leaves, then every warp tests them. Any other tile, or one
+// round holds `round_leaves` leaves, then every warp tests them. Any other tile, or one
 // whose beam was abandoned, is cast warp by warp in place (packet, or per
 // lane). Other batches are cast in 32-ray chunks, as k_trace_packets casts
 // them.
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kBeamRays, MINB)
                   uint32_t *__restrict__ counter, uint32_t *err, const uint32_t *__restrict__ perm,
                   uint32_t *__restrict__ list, uint32_t *__restrict__ list_count,
                   const uint32_t *__restrict__ cell_tiles, const uint32_t *__restrict__ cell_count,
-                  const uint32_t *__restrict__ ext, bool refine) {
+                  const uint32_t *__restrict__ ext, int round_leaves, bool refine) {
   __shared__ BeamShared s;
   extern __shared__ int s_dyn_stack[];  // STACK entries per warp (packet casts)
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kBeamRays, MINB)
       float maxd = INF;
       uint32_t steps = 0;
       for (;;) {
-        if (sp > 0 && nl < kBeamBatch) {
+        if (sp > 0 && nl < round_leaves) {
           if (++steps > sc.ntris + 16u) {
             if (tid == 0) atomicOr(err, KERR_TIMEOUT);
             beam = false;
@@ -890,7 +890,8 @@ cudaError_t launch_variant(const DevScene &sc, const rt_ray *rays, uint32_t n, r
         auto bk = k_trace_beams<STACK, 4>;
         const size_t smem = (size_t)(kBeamRays / 32) * STACK * sizeof(int);
         bk<<<persistent_grid(bk, n, kBeamRays, smem), kBeamRays, smem, st>>>(
-            sc, r4, n, h4, counter, err, perm, plist, chunk_scratch, cells->tiles, cells->count, cells->ext, refine);
+            sc, r4, n, h4, counter, err, perm, plist, chunk_scratch, cells->tiles, cells->count, cells->ext,
+            opts.beam_round, refine);
       } else {
         auto pk = opts.packet_minblocks >= 16   ? k_trace_packets<STACK, 16>
                   : opts.packet_minblocks >= 12 ? k_trace_packets<STACK, 12>
