@@ -178,7 +178,7 @@ rt_status rtTraceClosestHost(rt_ctx *ctx, rt_scene_id scene, const rt_ray *h_ray
  *                   to 256 rays (the sort's Morton cells) that walk the tree
  *                   once as a beam: the block expands the tile's cone, the
  *                   rays test the leaves it meets (each with its own slab
- *                   test first); 0 = warp packets; 2 (default) = beams on
+ *                   test first); 0 (default) = warp packets; 2 = beams on
  *                   Bvh.h's median-split tree (bvh.builder 0 or the caller's
  *                   nodes), whose overlapping boxes favour them, packets on
  *                   the LBVH and PLOC trees. Results are identical either way

@@ -410,7 +410,7 @@ def test_tuning_keys(rt, ctx):
     for key, bad in (("trace.beam", 3), ("trace.beam", -1), ("trace.beam_round", 15), ("trace.beam_round", 257)):
         with pytest.raises(rt.RtError):
             ctx.set_tuning(key, bad)
-    assert ctx.get_tuning("trace.beam") == 2 and ctx.get_tuning("trace.beam_round") == 64
+    assert ctx.get_tuning("trace.beam") == 0 and ctx.get_tuning("trace.beam_round") == 64
 
 
 @pytest.mark.parametrize("builder", [1, 2], ids=["lbvh", "ploc"])

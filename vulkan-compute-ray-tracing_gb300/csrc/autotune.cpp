@@ -101,7 +101,7 @@ rt_status rtAutotuneTrace(rt_ctx *ctx, rt_scene_id scene, const rt_ray *d_rays, 
                         {"trace.minblocks", {16, 12, 10}},
                         {"trace.packet_minblocks", {16, 12, 10}},
                         {"trace.sort", {1, 0}},
-                        {"trace.beam", {2, 0, 1}}};
+                        {"trace.beam", {0, 2, 1}}};
   float best = 0.0f;
   rt_status s = time_trace(ctx, scene, d_rays, n, d_hits, reps, &best);
   if (s != RT_SUCCESS) return s;

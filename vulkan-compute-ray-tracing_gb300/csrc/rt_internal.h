@@ -87,7 +87,7 @@ struct TraceOpts {
   int refill = 32;  // idle lanes per warp that trigger a fetch of new rays (32: whole-warp batches)
   int sort = 1;     // 1: cast rays in Morton order of origin and direction (raysort.cu)
   int packet = 1;   // 1: warps of coherent rays traverse as one packet (traverse_packet)
-  int beam = 2;     // sorted one-origin batches traverse the sort's cell tiles as beams (beam.cuh):
+  int beam = 0;     // sorted one-origin batches traverse the sort's cell tiles as beams (beam.cuh):
                     // 1 always, 0 never, 2 on Bvh.h's median-split trees (DevScene::median_tree)
   int beam_round = 64;  // leaves a beam round collects before its rays test them (16..256)
   int spec = 1;     // 1: per-lane traversal parks leaves until the whole warp holds one (traverse_spec)
