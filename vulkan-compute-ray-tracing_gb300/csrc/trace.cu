@@ -4,8 +4,11 @@
 // warp and traverses coherent ones as a packet, listing the rest, and
 // k_trace_wide casts the listed chunks one ray per lane over the 8-wide
 // tree with a shared leaf pool (k_trace_lanes: the same over the binary
-// layout with postponed leaves). k_trace is the per-lane refill form (a warp claims new rays as
-// lanes finish), k_trace_literal16 the shader's literal traversal.
+// layout with postponed leaves). With trace.beam, k_trace_beams takes the
+// first kernel's place for sorted batches: one-origin batches are cast per
+// Morton cell as beams (beam.cuh), others in 32-ray chunks as above.
+// k_trace is the per-lane refill form (a warp claims new rays as lanes
+// finish), k_trace_literal16 the shader's literal traversal.
 //
 // The hit is chosen with the reference's fp32 arithmetic (traverse.cuh).
 // Unless RT_HIT_FP32 is set, t, u, v of the chosen triangle are then
