@@ -114,7 +114,7 @@ __device__ __forceinline__ bool beam_step(BeamShared &s, const Cone &cone, const
   const int take = sp < kBeamRays ? sp : kBeamRays;
   const bool mine = j < take;
   const int node = mine ? s.stack[sp - 1 - j] : 0;
-  const bool bad = mine && (uint32_t)node >= sc.ntris - 1u;  // pair nodes are 0 .. ntris - 2
+  bool bad = mine && (uint32_t)node >= sc.ntris - 1u;  // pair nodes are 0 .. ntris - 2
   float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a, c = a, d = a;
   bool h0 = false, h1 = false;
   if (mine && !bad) {
@@ -123,6 +123,8 @@ __device__ __forceinline__ bool beam_step(BeamShared &s, const Cone &cone, const
     h1 = cone_box<ZA>(cone, c, d, maxd2);
   }
   const int r0 = __float_as_int(b.z), r1 = __float_as_int(d.z);
+  // Leaf refs ~k name a triangle record, k < ntris.
+  bad |= (h0 && r0 < 0 && (uint32_t)~r0 >= sc.ntris) || (h1 && r1 < 0 && (uint32_t)~r1 >= sc.ntris);
   const bool in0 = h0 && r0 >= 0, in1 = h1 && r1 >= 0, lf0 = h0 && r0 < 0, lf1 = h1 && r1 < 0;
   const uint32_t bi0 = __ballot_sync(0xffffffffu, in0), bi1 = __ballot_sync(0xffffffffu, in1);
   const uint32_t bl0 = __ballot_sync(0xffffffffu, lf0), bl1 = __ballot_sync(0xffffffffu, lf1);
