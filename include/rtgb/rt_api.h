@@ -272,7 +272,7 @@ rt_status rtGetTuning(rt_ctx *ctx, const char *key, int64_t *value);
  * compile time, ray-trace-compute.comp:3, 262). Times the closest-hit
  * launch shapes on the caller's own device rays (coordinate descent over
  * trace.block, trace.stack, trace.wide, trace.wide_minblocks, trace.wide_visits, trace.defer,
- * trace.spec, trace.minblocks, trace.packet_minblocks, trace.sort; `reps` timed casts
+ * trace.spec, trace.minblocks, trace.packet_minblocks, trace.sort, trace.beam; `reps` timed casts
  * per candidate after one warm-up) and keeps the fastest. Hits are identical
  * in every shape; d_hits receives them. The rates before and after tuning
  * are returned in Grays/s (either pointer may be NULL). Synchronous. */

@@ -1,4 +1,5 @@
-// Ray reordering for closest-hit casting ("trace.sort").
+// Ray reordering for closest-hit casting ("trace.sort") and, on request,
+// for the bounces of wavefront renders ("render.sort").
 //
 // Rays whose origins and directions are close visit the same BVH nodes; a
 // warp holding such rays diverges less and shares cache lines. The batch is
@@ -10,7 +11,9 @@
 // then reads rays through it and writes each hit back to its input slot.
 // Order inside a bucket is arbitrary; results do not depend on the order.
 // With a device-side count (d_n), only the first *d_n rays of the buffer
-// take part (the launch is sized for the buffer's capacity n).
+// take part (the launch is sized for the buffer's capacity n). On request
+// the sorted batch is also cut into cell tiles (RayCells) for the beam
+// caster.
 #include <cuda_runtime.h>
 
 #include "rt_internal.h"

@@ -258,7 +258,7 @@ cudaStream_t ctx_stream(rt_ctx *ctx);
 // True when a batch or a server step gives a job of these params to the
 // wavefront kernels (render.mode 1, or 2 and at least
 // render.batch_wavefront_pixels; never the 16-entry compat traversal);
-// *sort receives trace.sort.
+// *sort receives render.sort (the per-bounce reordering).
 bool ctx_wavefront_render(rt_ctx *ctx, const rt_render_params &p, bool *sort, bool *wide = nullptr,
                           uint32_t *min_tris = nullptr);
 // Device bytes rtUploadScene allocates for a scene of these counts.
